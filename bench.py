@@ -1,0 +1,325 @@
+"""Benchmark of the per-tick SIR agent step on one GB300.
+
+Workload (default): 10,000,000 agents on a Barabasi-Albert graph (m=4, seed 1,
+about 8.0e7 directed CSR entries), relabelled by a seeded 64-way locality
+partition (logical ids keep the original agent ids as RNG keys), 0.1 %
+initially infected, beta=0.03, gamma=0.07, per-infected-neighbour SIR, 200
+ticks. One step = one simulate(200) from the initial state.
+
+  value : agent-ticks/s with inputs resident in HBM (device timed, CUDA events)
+  e2e   : the same through the C ABI with host buffers (pinned): the initial
+          state is copied in and the final state read back every step
+  roofline : the dominant kernel's algorithmic bytes / its CUDA-event duration
+  cpu_baseline : the CPU port of the same tick (OpenMP, all host cores) on a
+                 bounded sample of ticks
+
+`--impl reference` times the reference's CPU implementation of this path. The
+reference runs its step only as a CuPy GPU kernel (its use_gpu=False flag is
+ignored), so its CPU implementation here is the C restatement of its tick in
+oracle/ on all host cores, on the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_AGENTS = 10_000_000
+BA_M = 4
+TICKS = 200
+BETA, GAMMA = 0.03, 0.07
+INFECTED_FRAC = 0.001
+SEED = 1
+PARTS = 64
+CODES = (1, 2, 3)
+
+
+def _env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def build_workload(n=N_AGENTS):
+    from sagesim_gb300 import graphs
+
+    off, idx = graphs.barabasi_albert(n, BA_M, SEED)
+    perm, _ = graphs.partition_relabel(off, idx, PARTS, SEED)
+    roff, ridx = graphs.permute_csr(off, idx, perm)
+    st = np.full(n, CODES[0], dtype=np.int32)
+    st[graphs.initial_infected(n, INFECTED_FRAC, SEED)] = CODES[1]
+    rst = np.empty_like(st)
+    rst[perm] = st
+    lids = np.empty(n, dtype=np.int64)
+    lids[perm] = np.arange(n, dtype=np.int64)  # logical id = original agent id
+    return roff, ridx, rst, lids
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self._t.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_port_rate(off, idx, st, lids, ticks, threads=0):
+    """Agent-ticks/s of the C port of the tick (oracle/) on the host cores."""
+    from oracle import oracle
+
+    oracle.lib()
+    t0 = time.perf_counter()
+    _, stats, _ = oracle.sir_run(2, off, idx, st, SEED, 0, ticks, BETA, GAMMA, CODES, lids=lids,
+                                 nthreads=threads)
+    dt = time.perf_counter() - t0
+    used = threads if threads > 0 else oracle.max_threads()
+    return (off.size - 1) * ticks / dt, dt, used, stats
+
+
+def run_reference(args):
+    rank = _env_int("RANK", 0)
+    if rank != 0:
+        return
+    off, idx, st, lids = build_workload()
+    sample = max(1, _env_int("SG_REF_TICKS", 10))
+    rates = []
+    for _ in range(max(args.warmup, 0)):
+        cpu_port_rate(off, idx, st, lids, 1)
+    for _ in range(args.steps):
+        r, dt, used, _ = cpu_port_rate(off, idx, st, lids, sample)
+        rates.append(r)
+    v = float(np.median(rates))
+    line = {
+        "impl": "reference", "metric": "SIR agent-ticks/s (BA 1e7, 200-tick simulate)", "value": v,
+        "unit": "agent-ticks/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": N_AGENTS * TICKS / v * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": "SIR per-infected-neighbour, BA n=1e7 m=4 seed 1, 64-way relabel, "
+                               "0.1% infected, beta 0.03 gamma 0.07, 200 ticks",
+                   "sample": "%d ticks per step from tick 0" % sample},
+        "cpu_baseline": {"value": v, "unit": "agent-ticks/s", "cores": used, "kind": "port",
+                         "sample": "%d ticks of the 200-tick run per step (C port of the reference "
+                                   "tick, OpenMP)" % sample},
+        "e2e": {"value": v, "unit": "agent-ticks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--strategy", default="count", choices=["count", "pull"])
+    ap.add_argument("--agents", type=int, default=N_AGENTS)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+
+    from sagesim_gb300 import Engine
+
+    world = _env_int("WORLD_SIZE", 1)
+    rank = _env_int("RANK", 0)
+    local = _env_int("LOCAL_RANK", 0)
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    n = args.agents
+    off, idx, st0, lids = build_workload(n)
+    nnz = int(off[-1])
+    stream = torch.cuda.current_stream()
+    eng = Engine(device=local, stream=stream.cuda_stream)
+    eng.set_graph(off, idx, symmetric=True)
+    eng.set_logical_ids(lids)
+    eng.set_seed(SEED)
+    prop = eng.add_property("state", np.int32, init=st0)
+    eng.add_sir(prop, BETA, GAMMA, variant="B", strategy=args.strategy, codes=CODES)
+    eng.snapshot()
+
+    # trajectory statistics (untimed): E_S per tick for edge-visits/s and bytes
+    tick_stats, tot = eng.run(0, TICKS, stats=True)
+    eng.restore()
+
+    def step():
+        eng.restore()
+        eng.run_async(0, TICKS, use_graph=True)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * n * TICKS / (ms_step / 1e3)
+
+    # end to end through the C ABI with pinned host buffers
+    h_in = torch.from_numpy(st0).pin_memory()
+    h_out = torch.empty(n, dtype=torch.int32).pin_memory()
+    for _ in range(2):
+        eng.set_property_ptr(prop, h_in.data_ptr(), 0, n)
+        eng.run_async(0, TICKS, use_graph=True)
+        eng.get_property_ptr(prop, h_out.data_ptr(), 0, n)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.set_property_ptr(prop, h_in.data_ptr(), 0, n)
+        eng.run_async(0, TICKS, use_graph=True)
+        eng.get_property_ptr(prop, h_out.data_ptr(), 0, n)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_value = world * n * TICKS / e2e_s
+
+    # dominant kernel: per-launch CUDA events (separate, profiled run)
+    eng.restore()
+    eng.profile(True)
+    eng.run(0, TICKS, stats=False)
+    rep = eng.profile_report()
+    eng.profile(False)
+    dom = max(rep.items(), key=lambda kv: kv[1][1])
+    dom_name, (dom_launches, dom_ms) = dom
+    S = tick_stats[:, 0].astype(np.float64)
+    S_start = np.concatenate([[float((st0 == CODES[0]).sum())], S[:-1]])
+    I = tick_stats[:, 1].astype(np.float64)
+    R = tick_stats[:, 2].astype(np.float64)
+    changes = np.abs(np.diff(np.concatenate([[float((st0 == CODES[2]).sum())], R]))) + \
+        np.abs(np.diff(np.concatenate([[float((st0 == CODES[0]).sum())], S])))
+    E_S = tick_stats[:, 3].astype(np.float64)
+    if dom_name == "sir_count_step":
+        # per tick: state read + state write (4 B each, all agents), infected-
+        # neighbour count read for S agents, change-list append
+        alg = 8.0 * n + 4.0 * S_start + 4.0 * changes
+    elif dom_name == "sir_count_scatter":
+        alg = 8.0 * changes  # change-list read + row offsets; atomics counted below
+    else:  # pull: 12 B per agent + 4 B per CSR entry of tick-start S agents
+        alg = 12.0 * n + 4.0 + 4.0 * E_S
+    alg_per_launch = float(alg.mean())
+    per_launch_ms = dom_ms / max(dom_launches, 1)
+    achieved = alg_per_launch / (per_launch_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    kernels_per_tick = 2 if args.strategy == "count" else 1
+    launches = args.steps * (TICKS * kernels_per_tick + (1 if args.strategy == "count" else 0))
+
+    cpu = None
+    if rank == 0:
+        sample = max(1, _env_int("SG_CPU_TICKS", 10))
+        rate, dt, used, _ = cpu_port_rate(off, idx, st0, lids, sample)
+        cpu = {"value": rate, "unit": "agent-ticks/s", "cores": used, "kind": "port",
+               "sample": "first %d ticks of the same workload (%.1f s), C port of the reference tick "
+                         "(oracle/), OpenMP" % (sample, dt)}
+
+    line = {
+        "metric": "SIR agent-ticks/s (BA 1e7, 200-tick simulate)", "value": value,
+        "unit": "agent-ticks/s", "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32", "data": "synthetic",
+        "config": {"workload": "SIR per-infected-neighbour (salt 2+j trials), BA n=%d m=4 seed 1, "
+                               "64-way locality relabel, 0.1%% infected, beta 0.03 gamma 0.07, 200 ticks"
+                               % n,
+                   "strategy": args.strategy, "nnz": nnz, "l2": "inputs larger than L2 (CSR %.0f MB)"
+                                                               % (nnz * 4 / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "edge_visits_per_s": world * float(E_S.sum()) / (ms_step / 1e3),
+        "e2e": {"value": e2e_value, "unit": "agent-ticks/s", "h2d_bytes_per_step": 4 * n,
+                "d2h_bytes_per_step": 4 * n},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "kernel": dom_name,
+                     "peak_source": peak_kind, "per_launch_us": per_launch_ms * 1e3,
+                     "alg_bytes_per_launch": alg_per_launch},
+        "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in rep.items()},
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

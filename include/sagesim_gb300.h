@@ -1,0 +1,212 @@
+/*
+ * sagesim_gb300.h -- C ABI of the GB300 engine for SAGESim's per-tick agent step.
+ *
+ * Conventions
+ *   - Every function returns an int status: SG_OK (0) or one of SG_ERR_*.
+ *     sg_last_error() gives the message of the last failure on a handle.
+ *   - Handles are opaque. The caller owns every host array it passes; the
+ *     engine copies what it keeps. The engine owns all device memory it
+ *     allocates and frees it in the matching *_destroy call.
+ *   - A handle is not thread-safe; one handle issues work on one CUDA stream
+ *     (the caller's, if given in sg_engine_cfg.stream, else its own).
+ *   - Agent indices and CSR offsets are int32: an engine holds fewer than
+ *     2^31 agents and 2^31 CSR entries.
+ *   - Philox draws are keyed exactly as SAGESim keys them
+ *     (sagesim/math_utils.py:106-189): counter (tick*1000003 + salt, logical id),
+ *     key = seed, all mod 2^32; u = (c0 mod 2^23) / 2^23.
+ *
+ * Reference interfaces replaced (file:line in the SAGESim source tree):
+ *   sg_engine_create/destroy      Model.__init__ / reset()      sagesim/model.py:357-386, 944-958
+ *   sg_set_graph_csr              NetworkSpace adjacency -> CSR sagesim/space.py:107-125,
+ *                                                               sagesim/internal_utils.py:111-186,
+ *                                                               sagesim/model.py:1143-1148
+ *   sg_set_logical_ids            set_agent_logical_id          sagesim/model.py:656-667, 1089-1096
+ *   sg_set_seed                   set_seed                      sagesim/model.py:652-654
+ *   sg_set_globals_f64            register/set_global_property  sagesim/model.py:588-604
+ *   sg_add_property               Breed.register_property +
+ *                                 property tensor upload        sagesim/breed.py:40-61,
+ *                                                               sagesim/model.py:1192-1197
+ *   sg_set_property/get_property  set/get_agent_property_value,
+ *                                 get_breed_data                sagesim/model.py:422-490
+ *   sg_add_builtin_step           register_step_func (builtin)  sagesim/breed.py:68-99
+ *   sg_compile_step               register_step_func + codegen  sagesim/breed.py:68-99,
+ *                                                               sagesim/model.py:2010-2457
+ *   sg_run                        simulate -> worker_coroutine  sagesim/model.py:961-998, 1314-1640
+ */
+#ifndef SAGESIM_GB300_H
+#define SAGESIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define SG_OK 0
+#define SG_ERR_INVALID 1   /* bad argument or call order                      */
+#define SG_ERR_BAD_CSR 2   /* offsets not monotone / index out of range       */
+#define SG_ERR_CUDA 3      /* a CUDA runtime call failed                      */
+#define SG_ERR_OOM 4       /* device allocation failed                        */
+#define SG_ERR_COMPILE 5   /* NVRTC rejected a step source (log in message)   */
+#define SG_ERR_BUDGET 6    /* request larger than the server's HBM budget     */
+#define SG_ERR_TIMEOUT 7   /* a bounded device-side wait gave up              */
+#define SG_ERR_OOB 8       /* a device bounds check fired (checked builds)    */
+#define SG_ERR_NOT_FOUND 9 /* unknown id                                      */
+
+/* ---- dtypes ------------------------------------------------------------ */
+#define SG_I32 0
+#define SG_F32 1
+
+/* ---- builtin steps ------------------------------------------------------ */
+/* SIR with one draw per agent per tick (SAGESim's own test step,
+ * tests/test_simulation.py:24-43). */
+#define SG_BUILTIN_SIR_A 1
+/* SIR with one Bernoulli(beta) trial per infected neighbour (salts 2, 3, ...). */
+#define SG_BUILTIN_SIR_B 2
+/* Opinion update: weighted mean of the first `width` ordered neighbours plus
+ * Philox N(0, sigma) noise, clamped to [0, 1]. */
+#define SG_BUILTIN_OPINION 3
+
+/* ---- SIR evaluation strategy (same results, different work) ---------------- */
+/* Pull: each susceptible agent scans its CSR row every tick (degree-binned:
+ * thread per agent, warp per hub). */
+#define SG_SIR_PULL 0
+/* Count: the engine keeps, per agent, the number of infected neighbours and
+ * updates it only for agents whose state changed (needs the transpose CSR,
+ * built once per graph). */
+#define SG_SIR_COUNT 1
+
+/* ---- graph flags ------------------------------------------------------------ */
+/* Row order matters (NetworkSpace(ordered=True), sagesim/space.py:54-71). */
+#define SG_GRAPH_ORDERED 1
+/* The caller asserts the CSR is symmetric (undirected graph); the count
+ * strategy then reuses it as its own transpose. */
+#define SG_GRAPH_SYMMETRIC 2
+
+typedef struct sg_engine sg_engine;
+
+typedef struct sg_engine_cfg {
+    int32_t device;  /* CUDA device ordinal                                   */
+    int32_t flags;   /* reserved, 0                                           */
+    void *stream;    /* cudaStream_t to issue work on; NULL = engine-owned     */
+} sg_engine_cfg;
+
+/* Parameters of a builtin step. Probabilities are float64 like SAGESim globals
+ * (sagesim/model.py:593); the kernel compares the 23-bit Philox integer against
+ * the exact integer threshold ceil(p * 2^23), which is the same test as the
+ * reference's double compare `u < p`. */
+typedef struct sg_builtin_params {
+    int32_t builtin;        /* SG_BUILTIN_*                                          */
+    int32_t strategy;       /* SIR: SG_SIR_PULL or SG_SIR_COUNT                       */
+    int32_t state_prop;     /* SIR: int32 state property; OPINION: float32 opinion    */
+    int32_t aux_prop;       /* OPINION: float32[width] weights property; else -1      */
+    int32_t code_s, code_i, code_r; /* SIR state codes (SAGESim tests use 1, 2, 3)  */
+    int32_t priority;       /* execution priority (lower runs first)                  */
+    int64_t begin, end;     /* agent range the step runs over (a breed's range)       */
+    double beta, gamma;     /* SIR probabilities                                      */
+    double sigma;           /* OPINION noise standard deviation                       */
+} sg_builtin_params;
+
+/* Per-run statistics. */
+typedef struct sg_stats {
+    int64_t ticks;          /* ticks executed                                   */
+    int64_t agent_ticks;    /* agents x ticks over the stepped ranges           */
+    int64_t edge_visits;    /* sum over ticks of E_S (degree sum of the agents
+                               susceptible at tick start); SIR only             */
+    double device_ms;       /* device time of the run (CUDA events)             */
+} sg_stats;
+
+/* ---- engine lifecycle ------------------------------------------------------- */
+int sg_engine_create(const sg_engine_cfg *cfg, sg_engine **out);
+int sg_engine_destroy(sg_engine *e);
+/* Copies the last error message of `e` (or of the last failed create when e is
+ * NULL) into buf (always NUL-terminated when cap > 0). */
+int sg_last_error(const sg_engine *e, char *buf, size_t cap);
+
+/* ---- model definition -------------------------------------------------------- */
+/* CSR of the agent graph: agent i's neighbours are indices[offsets[i] ..
+ * offsets[i+1]). Validates offsets[0] == 0, monotone offsets, offsets[n] == nnz
+ * and every index in [0, n); SG_ERR_BAD_CSR otherwise. Replaces any previous
+ * graph and fixes the agent count n. */
+int sg_set_graph_csr(sg_engine *e, const int32_t *offsets, int64_t n, const int32_t *indices,
+                     int64_t nnz, int32_t flags);
+/* RNG key per agent (default: the agent index). */
+int sg_set_logical_ids(sg_engine *e, const int64_t *lids, int64_t n);
+int sg_set_seed(sg_engine *e, int64_t seed);
+/* Global parameters visible to compiled step functions as `const double* g`. */
+int sg_set_globals_f64(sg_engine *e, const double *values, int32_t n);
+/* Adds a per-agent property of `width` values of `dtype`; init holds n*width
+ * values (NULL = zeros). `double_buffered` = 0 writes in place (SAGESim's
+ * no_double_buffer, sagesim/breed.py:68-99). */
+int sg_add_property(sg_engine *e, const char *name, int32_t dtype, int32_t width,
+                    int32_t double_buffered, const void *init, int32_t *prop_id);
+/* Host <-> device copies of agents [first, first+count) of a property. */
+int sg_set_property(sg_engine *e, int32_t prop, const void *host, int64_t first, int64_t count);
+int sg_get_property(sg_engine *e, int32_t prop, void *host, int64_t first, int64_t count);
+/* Device pointer of a property's current (read) buffer, for zero-copy callers. */
+int sg_property_device_ptr(sg_engine *e, int32_t prop, void **dptr);
+
+/* ---- steps --------------------------------------------------------------------- */
+int sg_add_builtin_step(sg_engine *e, const sg_builtin_params *p, int32_t *step_id);
+/* Replaces the parameters of a builtin step (same builtin and state property),
+ * e.g. after set_global_property_value (sagesim/model.py:599-604). */
+int sg_update_builtin_step(sg_engine *e, int32_t step_id, const sg_builtin_params *p);
+/* Compiles a CUDA C++ step with NVRTC and adds it at `priority` over agents
+ * [begin, end). `cuda_src` defines
+ *   __device__ void <entry>(const sg_ctx& ctx, int i)
+ * (sg_ctx is in sagesim_gb300_step.h, included automatically). written_props
+ * lists the properties the step writes. SG_ERR_COMPILE carries the NVRTC log. */
+int sg_compile_step(sg_engine *e, const char *cuda_src, const char *entry, int32_t priority,
+                    int64_t begin, int64_t end, const int32_t *written_props, int32_t n_written,
+                    int32_t *step_id);
+
+/* ---- execution ------------------------------------------------------------------ */
+/* Runs ticks [tick0, tick0 + nticks): per tick every priority in order, reads of
+ * double-buffered properties seeing tick-start values, then the write-back.
+ * tick_stats (nullable, host): 4 int64 per tick = S, I, R after the tick and E_S,
+ * summed over the SIR steps. out (nullable) gets totals. Synchronous. */
+int sg_run(sg_engine *e, int64_t tick0, int32_t nticks, int64_t *tick_stats, sg_stats *out);
+/* Same, asynchronous on the engine stream: returns after enqueueing (through a
+ * CUDA graph of the tick loop when use_graph != 0). No stats. */
+int sg_run_async(sg_engine *e, int64_t tick0, int32_t nticks, int32_t use_graph);
+int sg_synchronize(sg_engine *e);
+
+/* Device snapshot of every property (checkpoint in HBM) and restore. */
+int sg_snapshot(sg_engine *e);
+int sg_restore(sg_engine *e);
+
+/* Profiling: when enabled, sg_run brackets every kernel launch with CUDA events
+ * and accumulates time per kernel kind. */
+int sg_profile_enable(sg_engine *e, int32_t on);
+/* kind index -> name, launch count, total milliseconds; SG_ERR_NOT_FOUND past the end. */
+int sg_profile_get(sg_engine *e, int32_t kind, char *name, size_t cap, int64_t *launches,
+                   double *total_ms);
+
+/* ---- host-side workload utilities (no counterpart in the reference, which
+ * builds graphs with networkx and partitions with METIS:
+ * sagesim/generate_partition.py:24-69, sagesim/partition_utils.py:39-103) ---- */
+/* Undirected graphs as symmetric CSR without self loops or duplicate edges.
+ * Two-pass: call with offsets/indices NULL to get nnz, then with buffers. */
+int sg_graph_er(int64_t n, double p, uint64_t seed, int32_t *offsets, int32_t *indices,
+                int64_t *nnz);
+int sg_graph_ba(int64_t n, int32_t m, uint64_t seed, int32_t *offsets, int32_t *indices,
+                int64_t *nnz);
+/* Watts-Strogatz ring lattice (k neighbours) with rewiring probability p; rows
+ * list neighbours in edge-insertion order (NetworkSpace(ordered=True)). */
+int sg_graph_ws(int64_t n, int32_t k, double p, uint64_t seed, int32_t *offsets,
+                int32_t *indices, int64_t *nnz);
+/* Seeded k-way locality partition (graph growing from k seeds, balanced parts,
+ * BFS order inside a part). perm[old] = new index; part[new] (nullable) = part id. */
+int sg_partition_relabel(int64_t n, const int32_t *offsets, const int32_t *indices, int32_t k,
+                         uint64_t seed, int32_t *perm, int32_t *part);
+/* Applies perm (perm[old] = new) to a CSR: row new = perm[old] lists perm[nbr]
+ * in the original order. */
+int sg_csr_permute(int64_t n, const int32_t *offsets, const int32_t *indices,
+                   const int32_t *perm, int32_t *new_offsets, int32_t *new_indices);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SAGESIM_GB300_H */

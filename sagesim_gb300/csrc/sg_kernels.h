@@ -1,0 +1,73 @@
+// sg_kernels.h -- launch interface of the tick kernels (host side).
+//
+// All tick kernels walk a tile list: a tile is a range of consecutive agents
+// that belong to one segment (one SIR/opinion step over one scenario's agent
+// range). A plain engine has one segment; an ensemble batch has one segment per
+// scenario. Tick-invariant per-segment data lives in a device table; the only
+// per-tick kernel argument is r, the tick index relative to the start of the
+// run, so a captured CUDA graph of the tick loop needs no host updates.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define SG_TILE 2048       // agents per tile
+#define SG_SIR_THREADS 256 // threads per block of the tick kernels
+
+struct SgSeg {
+    int64_t tick0;          // segment's absolute tick at r == 0
+    int64_t end_tick;       // the segment does no work at ticks >= end_tick
+    const int64_t *lids;    // RNG key per (global) agent index; NULL -> i - lid_base
+    int32_t lid_base;       // global index of the segment's first agent
+    int32_t variant;        // 1 = SIR-A, 2 = SIR-B, 3 = opinion
+    uint32_t key;           // seed mod 2^32
+    uint32_t kinf, krec;    // integer thresholds (SIR)
+    int32_t cs, ci, cr;     // SIR state codes
+    int32_t par0;           // state at tick0 lives in buffer [par0] of the pair
+    int32_t width;          // opinion: weights per agent
+    double sigma;           // opinion: noise standard deviation
+    unsigned long long *stats; // NULL or [ticks][4] counters, row r
+    const float *weights;   // opinion: [n][width] (global agent index)
+};
+
+struct SgTile {
+    int32_t seg, begin, end, pad;
+};
+
+struct SgTickArgs {
+    const int32_t *off;     // CSR offsets (global agent index)
+    const int32_t *idx;     // CSR indices (global agent index)
+    void *buf0, *buf1;      // ping-pong state pair (int32 SIR / float32 opinion)
+    const SgSeg *segs;
+    const SgTile *tiles;
+    int32_t ntiles;
+    int32_t r;              // tick relative to the run start
+    int32_t hub_deg;        // pull: rows longer than this go warp-per-agent
+    // count strategy
+    int32_t *cnt;           // infected-neighbour count per agent
+    int32_t *changes;       // change list: agent index, ~agent for I->R
+    int32_t *nchanges;      // [ticks] counters, slot r
+    const int32_t *toff;    // transpose CSR (in-neighbours)
+    const int32_t *tidx;
+};
+
+// Launchers return cudaGetLastError() of the launch.
+// variant: 1 = SIR-A, 2 = SIR-B (all segments of one launch share it). stats
+// selects the instantiation that accumulates S/I/R counts and E_S into
+// seg.stats (segments with stats == NULL skip the flush).
+cudaError_t sg_launch_sir_pull(const SgTickArgs &a, int variant, bool stats, int grid,
+                               cudaStream_t st);
+cudaError_t sg_launch_sir_count_init(const SgTickArgs &a, int grid, cudaStream_t st);
+cudaError_t sg_launch_sir_count_step(const SgTickArgs &a, int variant, bool stats, int grid,
+                                     cudaStream_t st);
+cudaError_t sg_launch_sir_count_scatter(const SgTickArgs &a, int grid, cudaStream_t st);
+cudaError_t sg_launch_opinion(const SgTickArgs &a, int grid, cudaStream_t st);
+// Copies [begin, end) of `words` 32-bit words from src to dst (write-back of
+// agents outside a step's range).
+cudaError_t sg_launch_copy_words(const uint32_t *src, uint32_t *dst, int64_t n, cudaStream_t st);
+// Transpose of a CSR (n rows, entries < n): counts, exclusive scan, fill.
+// tmp needs n+1 int32. Row order of the result is not specified (the count
+// strategy only sums over it).
+cudaError_t sg_transpose_csr(const int32_t *off, const int32_t *idx, int64_t n, int64_t nnz,
+                             int32_t *toff, int32_t *tidx, int32_t *tmp, void *scan_tmp,
+                             size_t scan_tmp_bytes, cudaStream_t st);
+size_t sg_transpose_scan_bytes(int64_t n);
