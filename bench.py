@@ -78,7 +78,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
@@ -167,17 +167,39 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def profile_case(args):
+    """One simulate(200) through the engine, no timing: the command ncu wraps."""
+    from sagesim_gb300 import Engine
+
+    off, idx, st0, lids = build_workload(args.agents)
+    with Engine() as eng:
+        eng.set_graph(off, idx, symmetric=True)
+        eng.set_logical_ids(lids)
+        eng.set_seed(SEED)
+        prop = eng.add_property("state", np.int32, init=st0)
+        eng.add_sir(prop, BETA, GAMMA, variant="B", strategy=args.strategy, codes=CODES)
+        eng.run(0, TICKS, stats=False)
+        final = eng.get_property(prop)
+    print("profile case done: %d agents, %d ticks, %d infected or recovered at the end"
+          % (args.agents, TICKS, int((final != CODES[0]).sum())))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--strategy", default="count", choices=["count", "pull"])
     ap.add_argument("--agents", type=int, default=N_AGENTS)
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run one simulate(200) of --strategy and exit (for ncu captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.profile_case:
+        profile_case(args)
         return
 
     import torch
@@ -197,91 +219,112 @@ def main():
     n = args.agents
     off, idx, st0, lids = build_workload(n)
     nnz = int(off[-1])
-    stream = torch.cuda.current_stream()
-    eng = Engine(device=local, stream=stream.cuda_stream)
-    eng.set_graph(off, idx, symmetric=True)
-    eng.set_logical_ids(lids)
-    eng.set_seed(SEED)
-    prop = eng.add_property("state", np.int32, init=st0)
-    eng.add_sir(prop, BETA, GAMMA, variant="B", strategy=args.strategy, codes=CODES)
-    eng.snapshot()
-
-    # trajectory statistics (untimed): E_S per tick for edge-visits/s and bytes
-    tick_stats, tot = eng.run(0, TICKS, stats=True)
-    eng.restore()
-
-    def step():
-        eng.restore()
-        eng.run_async(0, TICKS, use_graph=True)
-
-    for _ in range(max(args.warmup, 3)):
-        step()
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    clk = ClockSampler(local)
-    clk.start()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    ev0.record(stream)
-    for _ in range(args.steps):
-        step()
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    clocks = clk.stop()
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    ms_step = ms / args.steps
-    value = world * n * TICKS / (ms_step / 1e3)
-
-    # end to end through the C ABI with pinned host buffers
-    h_in = torch.from_numpy(st0).pin_memory()
-    h_out = torch.empty(n, dtype=torch.int32).pin_memory()
-    for _ in range(2):
-        eng.set_property_ptr(prop, h_in.data_ptr(), 0, n)
-        eng.run_async(0, TICKS, use_graph=True)
-        eng.get_property_ptr(prop, h_out.data_ptr(), 0, n)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        eng.set_property_ptr(prop, h_in.data_ptr(), 0, n)
-        eng.run_async(0, TICKS, use_graph=True)
-        eng.get_property_ptr(prop, h_out.data_ptr(), 0, n)
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    e2e_value = world * n * TICKS / e2e_s
-
-    # dominant kernel: per-launch CUDA events (separate, profiled run)
-    eng.restore()
-    eng.profile(True)
-    eng.run(0, TICKS, stats=False)
-    rep = eng.profile_report()
-    eng.profile(False)
-    dom = max(rep.items(), key=lambda kv: kv[1][1])
-    dom_name, (dom_launches, dom_ms) = dom
-    S = tick_stats[:, 0].astype(np.float64)
-    S_start = np.concatenate([[float((st0 == CODES[0]).sum())], S[:-1]])
-    I = tick_stats[:, 1].astype(np.float64)
-    R = tick_stats[:, 2].astype(np.float64)
-    changes = np.abs(np.diff(np.concatenate([[float((st0 == CODES[2]).sum())], R]))) + \
-        np.abs(np.diff(np.concatenate([[float((st0 == CODES[0]).sum())], S])))
-    E_S = tick_stats[:, 3].astype(np.float64)
-    if dom_name == "sir_count_step":
-        # per tick: state read + state write (4 B each, all agents), infected-
-        # neighbour count read for S agents, change-list append
-        alg = 8.0 * n + 4.0 * S_start + 4.0 * changes
-    elif dom_name == "sir_count_scatter":
-        alg = 8.0 * changes  # change-list read + row offsets; atomics counted below
-    else:  # pull: 12 B per agent + 4 B per CSR entry of tick-start S agents
-        alg = 12.0 * n + 4.0 + 4.0 * E_S
-    alg_per_launch = float(alg.mean())
-    per_launch_ms = dom_ms / max(dom_launches, 1)
-    achieved = alg_per_launch / (per_launch_ms / 1e3) / 1e9
+    stream = torch.cuda.Stream(device=local)
     peak, peak_kind = peaks()
-    kernels_per_tick = 2 if args.strategy == "count" else 1
-    launches = args.steps * (TICKS * kernels_per_tick + (1 if args.strategy == "count" else 0))
+
+    def measure(strategy, steps, warmup):
+        """Times `steps` simulate(200) calls of one strategy on its own engine."""
+        with torch.cuda.stream(stream):
+            eng = Engine(device=local, stream=stream.cuda_stream)
+            eng.set_graph(off, idx, symmetric=True)
+            eng.set_logical_ids(lids)
+            eng.set_seed(SEED)
+            prop = eng.add_property("state", np.int32, init=st0)
+            eng.add_sir(prop, BETA, GAMMA, variant="B", strategy=strategy, codes=CODES)
+            eng.snapshot()
+            # trajectory statistics (untimed): E_S per tick for edge-visits/s and bytes
+            tick_stats, _ = eng.run(0, TICKS, stats=True)
+            final = eng.get_property(prop)
+            eng.restore()
+
+            def step():
+                eng.restore()
+                eng.run_async(0, TICKS, use_graph=True)
+
+            for _ in range(max(warmup, 3)):
+                step()
+            stream.synchronize()
+            if dist:
+                dist.barrier()
+            clk = ClockSampler(local)
+            clk.start()
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            stream.synchronize()
+            ev0.record(stream)
+            for _ in range(steps):
+                step()
+            ev1.record(stream)
+            stream.synchronize()
+            clocks = clk.stop()
+            ms = ev0.elapsed_time(ev1)
+            if dist:
+                t = torch.tensor([ms], device="cuda")
+                dist.all_reduce(t, op=dist.ReduceOp.MAX)
+                ms = float(t.item())
+            ms_step = ms / steps
+
+            # end to end through the C ABI with pinned host buffers
+            h_in = torch.from_numpy(st0).pin_memory()
+            h_out = torch.empty(n, dtype=torch.int32).pin_memory()
+            for _ in range(2):
+                eng.set_property_ptr(prop, h_in.data_ptr(), 0, n)
+                eng.run_async(0, TICKS, use_graph=True)
+                eng.get_property_ptr(prop, h_out.data_ptr(), 0, n)
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                eng.set_property_ptr(prop, h_in.data_ptr(), 0, n)
+                eng.run_async(0, TICKS, use_graph=True)
+                eng.get_property_ptr(prop, h_out.data_ptr(), 0, n)
+            e2e_s = (time.perf_counter() - t0) / steps
+            if not np.array_equal(h_out.numpy(), final):
+                raise RuntimeError("end-to-end result differs from the device-resident run")
+
+            # dominant kernel: per-launch CUDA events (separate, profiled run)
+            eng.restore()
+            eng.profile(True)
+            eng.run(0, TICKS, stats=False)
+            rep = eng.profile_report()
+            eng.profile(False)
+            eng.close()
+        dom_name, (dom_launches, dom_ms) = max(rep.items(), key=lambda kv: kv[1][1])
+        S = tick_stats[:, 0].astype(np.float64)
+        S_start = np.concatenate([[float((st0 == CODES[0]).sum())], S[:-1]])
+        R = tick_stats[:, 2].astype(np.float64)
+        R_start = np.concatenate([[float((st0 == CODES[2]).sum())], R[:-1]])
+        changes = (S_start - S) + (R - R_start)  # S->I and I->R transitions
+        E_S = tick_stats[:, 3].astype(np.float64)
+        if dom_name == "sir_count_step":
+            # state read for every agent, count read for tick-start S agents,
+            # state write + change-list entry per transition
+            alg = 4.0 * n + 4.0 * S_start + 8.0 * changes
+        elif dom_name == "sir_count_scatter":
+            alg = 4.0 * changes
+        else:  # pull: 12 B per agent + 4 B per CSR entry of tick-start S agents
+            alg = 12.0 * n + 4.0 + 4.0 * E_S
+        alg_per_launch = float(alg.mean())
+        per_launch_ms = dom_ms / max(dom_launches, 1)
+        achieved = alg_per_launch / (per_launch_ms / 1e3) / 1e9
+        kernels_per_tick = 2 if strategy == "count" else 1
+        return {
+            "value": world * n * TICKS / (ms_step / 1e3), "ms_per_step": ms_step,
+            "e2e": world * n * TICKS / e2e_s, "edge_visits_per_s": world * float(E_S.sum()) / (ms_step / 1e3),
+            "launches": steps * (TICKS * kernels_per_tick + (1 if strategy == "count" else 0)),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "kernel": dom_name,
+                         "peak_source": peak_kind, "per_launch_us": per_launch_ms * 1e3,
+                         "alg_bytes_per_launch": alg_per_launch},
+            "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in rep.items()},
+            "clocks": clocks, "final": final,
+        }
+
+    results = {}
+    for strategy in [args.strategy] + [s for s in ("count", "pull") if s != args.strategy]:
+        results[strategy] = measure(strategy, args.steps, args.warmup)
+    head = results[args.strategy]
+    for s_, r_ in results.items():
+        if not np.array_equal(r_["final"], head["final"]):
+            raise RuntimeError("strategies disagree on the final state")
 
     cpu = None
     if rank == 0:
@@ -292,31 +335,29 @@ def main():
                          "(oracle/), OpenMP" % (sample, dt)}
 
     line = {
-        "metric": "SIR agent-ticks/s (BA 1e7, 200-tick simulate)", "value": value,
+        "metric": "SIR agent-ticks/s (BA 1e7, 200-tick simulate)", "value": head["value"],
         "unit": "agent-ticks/s", "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
-        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "int32", "data": "synthetic",
+        "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
         "config": {"workload": "SIR per-infected-neighbour (salt 2+j trials), BA n=%d m=4 seed 1, "
                                "64-way locality relabel, 0.1%% infected, beta 0.03 gamma 0.07, 200 ticks"
                                % n,
-                   "strategy": args.strategy, "nnz": nnz, "l2": "inputs larger than L2 (CSR %.0f MB)"
-                                                               % (nnz * 4 / 1e6),
+                   "strategy": args.strategy, "nnz": nnz,
+                   "l2": "inputs larger than L2 (CSR %.0f MB)" % (nnz * 4 / 1e6),
                    "parallelism": "replicas" if world > 1 else "single"},
-        "edge_visits_per_s": world * float(E_S.sum()) / (ms_step / 1e3),
-        "e2e": {"value": e2e_value, "unit": "agent-ticks/s", "h2d_bytes_per_step": 4 * n,
+        "edge_visits_per_s": head["edge_visits_per_s"],
+        "e2e": {"value": head["e2e"], "unit": "agent-ticks/s", "h2d_bytes_per_step": 4 * n,
                 "d2h_bytes_per_step": 4 * n},
-        "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "kernel": dom_name,
-                     "peak_source": peak_kind, "per_launch_us": per_launch_ms * 1e3,
-                     "alg_bytes_per_launch": alg_per_launch},
-        "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in rep.items()},
-        "clocks": clocks,
+        "gpu_launches": head["launches"],
+        "roofline": head["roofline"],
+        "kernels": head["kernels"],
+        "clocks": head["clocks"],
         "cpu_baseline": cpu,
+        "strategies": {k: {kk: vv for kk, vv in v.items() if kk not in ("final", "clocks")}
+                       for k, v in results.items()},
     }
     if rank == 0:
         print(json.dumps(line))
-    eng.close()
     if dist:
         dist.destroy_process_group()
 

@@ -71,7 +71,7 @@ struct sg_engine {
     int32_t next_step_id = 0;
 
     // scratch of the count strategy and of per-tick statistics
-    SgDev cnt, changes, nchanges, stats;
+    SgDev cnt, changes, tile_nch, stats;
     SgDev transpose_tmp, scan_tmp;
     SgDev prop_table; // sg_prop_dev per property, for compiled steps
 
@@ -429,6 +429,7 @@ struct SgPlan {
     std::vector<int32_t> copy_props;         // double-buffered props needing copy-through
     std::vector<int32_t> swap_props;         // double-buffered props written this tick
     SgStep *count_step = nullptr;
+    bool count_inplace = false; // the count step is the only step: state updated in place
 };
 
 static SgPlan make_plan(sg_engine *e)
@@ -451,8 +452,10 @@ static SgPlan make_plan(sg_engine *e)
             s->bp.strategy == SG_SIR_COUNT)
             pl.count_step = s;
     }
+    pl.count_inplace = pl.count_step != nullptr && pl.order.size() == 1;
     for (size_t p = 0; p < e->props.size(); ++p) {
         if (!written[p]) continue;
+        if (pl.count_inplace && (int32_t)p == pl.count_step->bp.state_prop) continue;
         pl.swap_props.push_back((int32_t)p);
         if (!(written[p] == 1 && fully[p] == 1)) pl.copy_props.push_back((int32_t)p);
     }
@@ -516,15 +519,15 @@ static int ensure_transpose(sg_engine *e)
     return SG_OK;
 }
 
-static SgTickArgs base_args(sg_engine *e, SgStep *s, int32_t r)
+static SgTickArgs base_args(sg_engine *e, SgStep *s, int32_t r, bool inplace)
 {
     SgTickArgs a{};
     a.off = e->off.as<int32_t>();
     a.idx = e->idx.as<int32_t>();
     if (s->kind != 0) {
         SgProp &sp = *e->props[s->bp.state_prop];
-        a.buf0 = sp.buf[0].p;
-        a.buf1 = sp.buf[1].p;
+        a.buf0 = inplace ? sp.buf[sp.cur].p : sp.buf[0].p;
+        a.buf1 = inplace ? sp.buf[sp.cur].p : sp.buf[1].p;
     }
     a.segs = s->seg.as<SgSeg>();
     a.tiles = s->tiles.as<SgTile>();
@@ -533,7 +536,7 @@ static SgTickArgs base_args(sg_engine *e, SgStep *s, int32_t r)
     a.hub_deg = e->hub_deg;
     a.cnt = e->cnt.as<int32_t>();
     a.changes = e->changes.as<int32_t>();
-    a.nchanges = e->nchanges.as<int32_t>();
+    a.tile_nch = e->tile_nch.as<int32_t>();
     const bool sym = (e->graph_flags & SG_GRAPH_SYMMETRIC) != 0;
     a.toff = sym ? e->off.as<int32_t>() : e->toff.as<int32_t>();
     a.tidx = sym ? e->idx.as<int32_t>() : e->tidx.as<int32_t>();
@@ -563,8 +566,7 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
     const int grid_sc = e->sm_count * 4;
     if (pl.count_step) {
         SgStep *s = pl.count_step;
-        SG_CK(cudaMemsetAsync(e->nchanges.p, 0, (size_t)std::max(nticks, 1) * 4, e->stream));
-        SgTickArgs a = base_args(e, s, 0);
+        SgTickArgs a = base_args(e, s, 0, pl.count_inplace);
         SG_PROF_LAUNCH("sir_count_init", sg_launch_sir_count_init(a, grid_for(e, s->ntiles), e->stream));
     }
     for (int32_t r = 0; r < nticks; ++r) {
@@ -576,12 +578,13 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
                                                 e->n * pp.width, e->stream));
         }
         for (SgStep *s : pl.order) {
-            SgTickArgs a = base_args(e, s, r);
+            const bool inplace = pl.count_inplace && s == pl.count_step;
+            SgTickArgs a = base_args(e, s, r, inplace);
             const int grid = grid_for(e, s->ntiles);
             if (s->kind == SG_BUILTIN_SIR_A || s->kind == SG_BUILTIN_SIR_B) {
                 const int variant = s->kind == SG_BUILTIN_SIR_A ? 1 : 2;
                 if (s->bp.strategy == SG_SIR_COUNT) {
-                    SG_PROF_LAUNCH("sir_count_step", sg_launch_sir_count_step(a, variant, stats_on, grid, e->stream));
+                    SG_PROF_LAUNCH("sir_count_step", sg_launch_sir_count_step(a, variant, stats_on, inplace, grid, e->stream));
                     SG_PROF_LAUNCH("sir_count_scatter", sg_launch_sir_count_scatter(a, grid_sc, e->stream));
                 } else {
                     SG_PROF_LAUNCH("sir_pull", sg_launch_sir_pull(a, variant, stats_on, grid, e->stream));
@@ -636,7 +639,6 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
         if (rc) return rc;
         SG_CK(e->cnt.reserve((size_t)std::max<int64_t>(e->n, 1) * 4));
         SG_CK(e->changes.reserve((size_t)std::max<int64_t>(e->n, 1) * 4));
-        SG_CK(e->nchanges.reserve((size_t)std::max(nticks, 1) * 4));
     }
     {
         // property views of compiled steps; cur0 fixes the parity at r == 0
@@ -653,6 +655,8 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
         rc = prepare_step(e, s, tick0, stats);
         if (rc) return rc;
     }
+    if (pl.count_step)
+        SG_CK(e->tile_nch.reserve((size_t)std::max(pl.count_step->ntiles, 1) * 4));
     return SG_OK;
 }
 

@@ -65,75 +65,182 @@ __device__ __forceinline__ uint32_t seg_lid(const SgSeg &sg, int32_t i)
     return sg.lids ? (uint32_t)(uint64_t)sg.lids[i] : (uint32_t)(i - sg.lid_base);
 }
 
-// ---- pull strategy ------------------------------------------------------------
+// ---- neighbour scans ------------------------------------------------------------
+// Every scan is counted, never ordered: SIR-A needs "any infected neighbour",
+// SIR-B needs only how many of the scanned neighbours are infected (the j-th
+// infected one draws salt 2 + j whichever neighbour it is). So rows are read
+// in batches whose loads are all independent (memory-level parallelism), and
+// the draws for a batch's c infected neighbours are tested together.
+//
+// Three bins by row length: a thread scans rows of <= kThreadRow entries
+// (4 independent gathers per step), a warp scans rows of <= kWarpRow entries
+// (128 per step), the whole block scans longer rows (1024 per step).
+constexpr int kBatch = 4;
+constexpr int32_t kThreadRow = 32;
+constexpr int32_t kWarpRow = 2048;
 
-// SIR-A (tests/test_simulation.py:24-43): infected iff u < beta and any
-// neighbour is infected. u was drawn by the caller; this only scans.
-__device__ __forceinline__ bool any_infected_thread(const int32_t *__restrict__ idx,
-                                                    const int32_t *__restrict__ sin, int32_t b,
-                                                    int32_t e, int32_t ci)
+// Number of infected entries among row[k .. min(k+4, e)), e > k.
+__device__ __forceinline__ int batch_count(const int32_t *__restrict__ idx,
+                                           const int32_t *__restrict__ sin, int32_t k, int32_t e,
+                                           int32_t ci)
 {
-    for (int32_t k = b; k < e; ++k)
-        if (__ldg(sin + __ldg(idx + k)) == ci) return true;
-    return false;
+    const int32_t last = e - 1;
+    const int32_t n0 = __ldg(idx + k);
+    const int32_t n1 = __ldg(idx + min(k + 1, last));
+    const int32_t n2 = __ldg(idx + min(k + 2, last));
+    const int32_t n3 = __ldg(idx + min(k + 3, last));
+    const int32_t s0 = __ldg(sin + n0), s1 = __ldg(sin + n1), s2 = __ldg(sin + n2),
+                  s3 = __ldg(sin + n3);
+    return (s0 == ci) + (k + 1 < e && s1 == ci) + (k + 2 < e && s2 == ci) + (k + 3 < e && s3 == ci);
 }
 
-__device__ __forceinline__ bool any_infected_warp(const int32_t *__restrict__ idx,
-                                                  const int32_t *__restrict__ sin, int32_t b,
-                                                  int32_t e, int32_t ci, int lane)
-{
-    for (int32_t k0 = b; k0 < e; k0 += 32) {
-        const int32_t k = k0 + lane;
-        const bool hit = (k < e) && (__ldg(sin + __ldg(idx + k)) == ci);
-        if (__any_sync(FULL_MASK, hit)) return true;
-    }
-    return false;
-}
-
-// SIR-B: the j-th infected neighbour found draws philox(salt 2 + j); any draw
-// below beta infects. Only the number of infected neighbours matters, so the
-// warp version counts 32 at a time and tests the next c draws in parallel.
+// SIR-B outcome for one agent from its row, thread path.
 __device__ __forceinline__ bool trials_thread(const int32_t *__restrict__ idx,
                                               const int32_t *__restrict__ sin, int32_t b,
                                               int32_t e, int32_t ci, uint32_t c0b, uint32_t lid,
                                               uint32_t key, uint32_t kinf)
 {
     uint32_t j = 0;
-    for (int32_t k = b; k < e; ++k) {
-        if (__ldg(sin + __ldg(idx + k)) == ci) {
+    for (int32_t k = b; k < e; k += kBatch) {
+        const int c = batch_count(idx, sin, k, e, ci);
+        for (int q = 0; q < c; ++q, ++j)
             if (sg_philox_k23(c0b + 2u + j, lid, key) < kinf) return true;
-            ++j;
-        }
     }
     return false;
 }
 
-__device__ __forceinline__ bool trials_warp(const int32_t *__restrict__ idx,
-                                            const int32_t *__restrict__ sin, int32_t b, int32_t e,
-                                            int32_t ci, uint32_t c0b, uint32_t lid, uint32_t key,
-                                            uint32_t kinf, int lane)
+__device__ __forceinline__ bool any_infected_thread(const int32_t *__restrict__ idx,
+                                                    const int32_t *__restrict__ sin, int32_t b,
+                                                    int32_t e, int32_t ci)
+{
+    for (int32_t k = b; k < e; k += kBatch)
+        if (batch_count(idx, sin, k, e, ci)) return true;
+    return false;
+}
+
+__device__ __forceinline__ int32_t count_thread(const int32_t *__restrict__ idx,
+                                                const int32_t *__restrict__ sin, int32_t b,
+                                                int32_t e, int32_t ci)
+{
+    int32_t c = 0;
+    for (int32_t k = b; k < e; k += kBatch) c += batch_count(idx, sin, k, e, ci);
+    return c;
+}
+
+// Warp path: each lane takes 4 entries per step (128 per warp step).
+__device__ __forceinline__ int warp_batch_count(const int32_t *__restrict__ idx,
+                                                const int32_t *__restrict__ sin, int32_t k0,
+                                                int32_t e, int32_t ci, int lane)
+{
+    const int32_t k = k0 + lane;
+    const bool v0 = k < e, v1 = k + 32 < e, v2 = k + 64 < e, v3 = k + 96 < e;
+    const int32_t last = e - 1;
+    const int32_t n0 = __ldg(idx + min(k, last));
+    const int32_t n1 = __ldg(idx + min(k + 32, last));
+    const int32_t n2 = __ldg(idx + min(k + 64, last));
+    const int32_t n3 = __ldg(idx + min(k + 96, last));
+    const int32_t s0 = __ldg(sin + n0), s1 = __ldg(sin + n1), s2 = __ldg(sin + n2),
+                  s3 = __ldg(sin + n3);
+    const int mine = (v0 && s0 == ci) + (v1 && s1 == ci) + (v2 && s2 == ci) + (v3 && s3 == ci);
+    int c = mine;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(FULL_MASK, c, o);
+    return c;
+}
+
+// Tests draws j0 .. j0+c-1 (salt 2 + j) across the warp; true if any is below beta.
+__device__ __forceinline__ bool warp_draws(uint32_t j0, int c, uint32_t c0b, uint32_t lid,
+                                           uint32_t key, uint32_t kinf, int lane)
+{
+    for (int q0 = 0; q0 < c; q0 += 32) {
+        const bool ok = (q0 + lane < c) &&
+                        (sg_philox_k23(c0b + 2u + j0 + (uint32_t)(q0 + lane), lid, key) < kinf);
+        if (__any_sync(FULL_MASK, ok)) return true;
+    }
+    return false;
+}
+
+// VARIANT 1: any infected; 2: SIR-B trials; 0: count (returned through *count).
+template <int VARIANT>
+__device__ __forceinline__ bool warp_row(const int32_t *__restrict__ idx,
+                                         const int32_t *__restrict__ sin, int32_t b, int32_t e,
+                                         int32_t ci, uint32_t c0b, uint32_t lid, uint32_t key,
+                                         uint32_t kinf, int lane, int32_t *count)
 {
     uint32_t j = 0;
-    for (int32_t k0 = b; k0 < e; k0 += 32) {
-        const int32_t k = k0 + lane;
-        const bool hit = (k < e) && (__ldg(sin + __ldg(idx + k)) == ci);
-        const unsigned m = __ballot_sync(FULL_MASK, hit);
-        if (m) {
-            const uint32_t c = (uint32_t)__popc(m);
-            const bool ok = ((uint32_t)lane < c) &&
-                            (sg_philox_k23(c0b + 2u + j + (uint32_t)lane, lid, key) < kinf);
-            if (__any_sync(FULL_MASK, ok)) return true;
-            j += c;
+    for (int32_t k0 = b; k0 < e; k0 += 128) {
+        const int c = warp_batch_count(idx, sin, k0, e, ci, lane);
+        if (VARIANT == 1 && c) return true;
+        if (VARIANT == 2 && c) {
+            if (warp_draws(j, c, c0b, lid, key, kinf, lane)) return true;
         }
+        j += (uint32_t)c;
     }
+    if (count) *count = (int32_t)j;
     return false;
 }
 
+// Block path for the longest rows: 256 threads x 4 entries per step; the
+// result is broadcast through __syncthreads_or / a shared counter.
+template <int VARIANT>
+__device__ __forceinline__ bool block_row(const int32_t *__restrict__ idx,
+                                          const int32_t *__restrict__ sin, int32_t b, int32_t e,
+                                          int32_t ci, uint32_t c0b, uint32_t lid, uint32_t key,
+                                          uint32_t kinf, int32_t *sh_count, int32_t *count)
+{
+    const int tid = threadIdx.x;
+    if (tid == 0) *sh_count = 0;
+    __syncthreads();
+    for (int32_t k0 = b; k0 < e; k0 += 4 * SG_SIR_THREADS) {
+        const int32_t k = k0 + tid;
+        const int32_t last = e - 1;
+        const int32_t n0 = __ldg(idx + min(k, last));
+        const int32_t n1 = __ldg(idx + min(k + SG_SIR_THREADS, last));
+        const int32_t n2 = __ldg(idx + min(k + 2 * SG_SIR_THREADS, last));
+        const int32_t n3 = __ldg(idx + min(k + 3 * SG_SIR_THREADS, last));
+        const int mine = (k < e && __ldg(sin + n0) == ci) +
+                         (k + SG_SIR_THREADS < e && __ldg(sin + n1) == ci) +
+                         (k + 2 * SG_SIR_THREADS < e && __ldg(sin + n2) == ci) +
+                         (k + 3 * SG_SIR_THREADS < e && __ldg(sin + n3) == ci);
+        if (mine) atomicAdd(sh_count, mine);
+        if (VARIANT == 1) {
+            if (__syncthreads_or(mine != 0)) return true;
+        }
+    }
+    __syncthreads();
+    const int32_t total = *sh_count;
+    if (count) *count = total;
+    if (VARIANT == 2) {
+        bool ok = false;
+        for (int32_t q = tid; q < total && !ok; q += SG_SIR_THREADS)
+            ok = sg_philox_k23(c0b + 2u + (uint32_t)q, lid, key) < kinf;
+        return __syncthreads_or(ok) != 0;
+    }
+    __syncthreads();
+    return false;
+}
+
+// Shared-memory queues of deferred rows for one 256-agent chunk.
+struct HubQueues {
+    int32_t warpq[SG_SIR_THREADS];
+    int32_t blockq[SG_SIR_THREADS];
+    int32_t nwarp, nblock;
+    int32_t count;
+};
+
+__device__ __forceinline__ void defer_row(HubQueues &q, int32_t i, int32_t deg)
+{
+    if (deg > kWarpRow)
+        q.blockq[atomicAdd(&q.nblock, 1)] = i;
+    else
+        q.warpq[atomicAdd(&q.nwarp, 1)] = i;
+}
+
+// ---- pull strategy --------------------------------------------------------------
 template <int VARIANT, bool STATS>
 __global__ void __launch_bounds__(SG_SIR_THREADS) sir_pull_kernel(SgTickArgs a)
 {
-    __shared__ int32_t hubq[SG_SIR_THREADS];
-    __shared__ int32_t hubn;
+    __shared__ HubQueues hq;
     __shared__ unsigned long long red[4][kWarps];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int32_t *__restrict__ off = a.off;
@@ -153,7 +260,10 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_pull_kernel(SgTickArgs a)
         unsigned long long nS = 0, nI = 0, nR = 0, eS = 0;
 
         for (int32_t base = tile.begin; base < tile.end; base += SG_SIR_THREADS) {
-            if (tid == 0) hubn = 0;
+            if (tid == 0) {
+                hq.nwarp = 0;
+                hq.nblock = 0;
+            }
             __syncthreads();
             const int32_t i = base + tid;
             if (i < tile.end) {
@@ -164,28 +274,19 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_pull_kernel(SgTickArgs a)
                     if (sg_philox_k23(c0b + 1u, seg_lid(sg, i), key) < krec) out = cr;
                 } else if (s == cs) {
                     const uint32_t lid = seg_lid(sg, i);
-                    if (VARIANT == 1) {
-                        const bool lucky = sg_philox_k23(c0b + 1u, lid, key) < kinf;
-                        if (lucky || STATS) {
-                            const int32_t b = __ldg(off + i), e = __ldg(off + i + 1);
-                            if (STATS) eS += (unsigned long long)(e - b);
-                            if (lucky) {
-                                if (e - b > a.hub_deg) {
-                                    deferred = true;
-                                    hubq[atomicAdd(&hubn, 1)] = i;
-                                } else if (any_infected_thread(idx, sin, b, e, ci)) {
-                                    out = ci;
-                                }
-                            }
-                        }
-                    } else {
+                    const bool lucky = VARIANT == 2 || sg_philox_k23(c0b + 1u, lid, key) < kinf;
+                    if (lucky || STATS) {
                         const int32_t b = __ldg(off + i), e = __ldg(off + i + 1);
                         if (STATS) eS += (unsigned long long)(e - b);
-                        if (e - b > a.hub_deg) {
-                            deferred = true;
-                            hubq[atomicAdd(&hubn, 1)] = i;
-                        } else if (trials_thread(idx, sin, b, e, ci, c0b, lid, key, kinf)) {
-                            out = ci;
+                        if (lucky) {
+                            if (e - b > kThreadRow) {
+                                deferred = true;
+                                defer_row(hq, i, e - b);
+                            } else if (VARIANT == 1 ? any_infected_thread(idx, sin, b, e, ci)
+                                                    : trials_thread(idx, sin, b, e, ci, c0b, lid,
+                                                                    key, kinf)) {
+                                out = ci;
+                            }
                         }
                     }
                 }
@@ -199,26 +300,32 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_pull_kernel(SgTickArgs a)
                 }
             }
             __syncthreads();
-            const int nh = hubn;
-            for (int q = warp; q < nh; q += kWarps) {
-                const int32_t h = hubq[q];
-                const int32_t b = __ldg(off + h), e = __ldg(off + h + 1);
-                bool inf;
-                if (VARIANT == 1)
-                    inf = any_infected_warp(idx, sin, b, e, ci, lane);
-                else
-                    inf = trials_warp(idx, sin, b, e, ci, c0b, seg_lid(sg, h), key, kinf, lane);
-                const int32_t out = inf ? ci : cs;
+            const int nw = hq.nwarp, nb = hq.nblock;
+            for (int q = warp; q < nw; q += kWarps) {
+                const int32_t h = hq.warpq[q];
+                const bool inf = warp_row<VARIANT>(idx, sin, __ldg(off + h), __ldg(off + h + 1), ci,
+                                                   c0b, seg_lid(sg, h), key, kinf, lane, nullptr);
                 if (lane == 0) {
-                    sout[h] = out;
+                    sout[h] = inf ? ci : cs;
                     if (STATS) {
-                        nS += (out == cs);
-                        nI += (out == ci);
+                        nS += !inf;
+                        nI += inf;
                     }
                 }
             }
-            // the next iteration's hubn reset is ordered after this read by its
-            // __syncthreads only if every thread has read hubn: sync here.
+            for (int q = 0; q < nb; ++q) {
+                const int32_t h = hq.blockq[q];
+                const bool inf = block_row<VARIANT>(idx, sin, __ldg(off + h), __ldg(off + h + 1), ci,
+                                                    c0b, seg_lid(sg, h), key, kinf, &hq.count,
+                                                    nullptr);
+                if (tid == 0) {
+                    sout[h] = inf ? ci : cs;
+                    if (STATS) {
+                        nS += !inf;
+                        nI += inf;
+                    }
+                }
+            }
             __syncthreads();
         }
         if (STATS && sg.stats) block_flush4(nS, nI, nR, eS, sg.stats + 4 * (int64_t)a.r, red);
@@ -226,67 +333,83 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_pull_kernel(SgTickArgs a)
 }
 
 // ---- count strategy -------------------------------------------------------------
-// cnt[i] = number of infected agents in row i. A susceptible agent then needs
-// only cnt[i]: SIR-A infects iff cnt > 0 and u < beta, SIR-B iff one of the
-// draws salt 2 .. 2+cnt-1 is below beta. Agents whose infected status changed
-// this tick are appended to a change list; the scatter kernel then adds +-1 to
-// cnt over their transpose rows (the agents that list them as neighbours).
+// cnt[i] = number of infected agents in row i, kept for susceptible agents
+// (the only ones that read it; agents never return to S). A susceptible agent
+// then needs only cnt[i]: SIR-A infects iff cnt > 0 and u < beta, SIR-B iff
+// one of the draws salt 2 .. 2+cnt-1 is below beta. Agents whose infected
+// status changed are appended to their tile's slice of the change list
+// (tile t owns changes[tile.begin ..] and tile_nch[t]; no global atomics);
+// the scatter kernel then adds +-1 to cnt along their transpose rows.
 
 __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_init_kernel(SgTickArgs a)
 {
-    const int lane = threadIdx.x & 31;
+    __shared__ HubQueues hq;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
         const SgTile tile = a.tiles[t];
         const SgSeg &sg = a.segs[tile.seg];
         const int par = sg.par0 & 1;
         const int32_t *__restrict__ sin = (const int32_t *)(par ? a.buf1 : a.buf0);
-        const int32_t ci = sg.ci;
-        // one warp per agent: rows of any length, coalesced
-        for (int32_t i = tile.begin + (int32_t)(threadIdx.x >> 5); i < tile.end; i += kWarps) {
-            const int32_t b = a.off[i], e = a.off[i + 1];
-            int32_t c = 0;
-            for (int32_t k = b + lane; k < e; k += 32) c += (sin[a.idx[k]] == ci);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(FULL_MASK, c, o);
-            if (lane == 0) a.cnt[i] = c;
+        const int32_t ci = sg.ci, cs = sg.cs;
+        for (int32_t base = tile.begin; base < tile.end; base += SG_SIR_THREADS) {
+            if (tid == 0) {
+                hq.nwarp = 0;
+                hq.nblock = 0;
+            }
+            __syncthreads();
+            const int32_t i = base + tid;
+            if (i < tile.end && sin[i] == cs) {
+                const int32_t b = a.off[i], e = a.off[i + 1];
+                if (e - b > kThreadRow)
+                    defer_row(hq, i, e - b);
+                else
+                    a.cnt[i] = count_thread(a.idx, sin, b, e, ci);
+            }
+            __syncthreads();
+            const int nw = hq.nwarp, nb = hq.nblock;
+            for (int q = warp; q < nw; q += kWarps) {
+                const int32_t h = hq.warpq[q];
+                int32_t c = 0;
+                warp_row<0>(a.idx, sin, a.off[h], a.off[h + 1], ci, 0, 0, 0, 0, lane, &c);
+                if (lane == 0) a.cnt[h] = c;
+            }
+            for (int q = 0; q < nb; ++q) {
+                const int32_t h = hq.blockq[q];
+                int32_t c = 0;
+                block_row<0>(a.idx, sin, a.off[h], a.off[h + 1], ci, 0, 0, 0, 0, &hq.count, &c);
+                if (tid == 0) a.cnt[h] = c;
+            }
+            __syncthreads();
         }
     }
 }
 
-__device__ __forceinline__ void push_change(int32_t *changes, int32_t *counter, bool has,
-                                            int32_t code)
-{
-    const unsigned m = __ballot_sync(FULL_MASK, has);
-    if (!m) return;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(m) - 1;
-    int32_t base = 0;
-    if (lane == leader) base = atomicAdd(counter, __popc(m));
-    base = __shfl_sync(FULL_MASK, base, leader);
-    if (has) changes[base + __popc(m & ((1u << lane) - 1u))] = code;
-}
-
-template <int VARIANT, bool STATS>
+template <int VARIANT, bool STATS, bool INPLACE>
 __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickArgs a)
 {
     __shared__ unsigned long long red[4][kWarps];
-    const int tid = threadIdx.x;
-    int32_t *counter = a.nchanges + a.r;
+    __shared__ int32_t nch;
+    const int tid = threadIdx.x, lane = tid & 31;
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
         const SgTile tile = a.tiles[t];
         const SgSeg &sg = a.segs[tile.seg];
         const int64_t tick = sg.tick0 + a.r;
-        if (tick >= sg.end_tick) continue;
-        const int par = (sg.par0 + a.r) & 1;
-        const int32_t *__restrict__ sin = (const int32_t *)(par ? a.buf1 : a.buf0);
-        int32_t *__restrict__ sout = (int32_t *)(par ? a.buf0 : a.buf1);
+        if (tick >= sg.end_tick) {
+            if (tid == 0) a.tile_nch[t] = 0;
+            continue;
+        }
+        const int par = INPLACE ? 0 : ((sg.par0 + a.r) & 1);
+        const int32_t *sin = (const int32_t *)(par ? a.buf1 : a.buf0);
+        int32_t *sout = (int32_t *)(INPLACE ? a.buf0 : (par ? a.buf0 : a.buf1));
         const uint32_t c0b = sg_c0base(tick);
         const uint32_t key = sg.key, kinf = sg.kinf, krec = sg.krec;
         const int32_t cs = sg.cs, ci = sg.ci, cr = sg.cr;
+        int32_t *tchanges = a.changes + tile.begin;
         unsigned long long nS = 0, nI = 0, nR = 0, eS = 0;
-        // tile.end - tile.begin is a multiple of the block size except for the
-        // segment's last tile; the loop keeps every lane of a warp alive for
-        // the ballot in push_change.
+        if (tid == 0) nch = 0;
+        __syncthreads();
+        // every thread runs the same number of iterations: the ballot below
+        // needs all 32 lanes
         for (int32_t base = tile.begin; base < tile.end; base += SG_SIR_THREADS) {
             const int32_t i = base + tid;
             bool has = false;
@@ -301,7 +424,7 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickAr
                         code = ~i;
                     }
                 } else if (s == cs) {
-                    if (STATS) eS += (unsigned long long)(a.off[i + 1] - a.off[i]);
+                    if (STATS) eS += (unsigned long long)(__ldg(a.off + i + 1) - __ldg(a.off + i));
                     const int32_t k = a.cnt[i];
                     if (k > 0) {
                         const uint32_t lid = seg_lid(sg, i);
@@ -323,16 +446,26 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickAr
                         }
                     }
                 }
-                sout[i] = out;
+                if (!INPLACE || has) sout[i] = out;
                 if (STATS) {
                     nS += (out == cs);
                     nI += (out == ci);
                     nR += (out == cr);
                 }
             }
-            push_change(a.changes, counter, has, code);
+            const unsigned m = __ballot_sync(FULL_MASK, has);
+            if (m) {
+                const int leader = __ffs(m) - 1;
+                int32_t pos = 0;
+                if (lane == leader) pos = atomicAdd(&nch, __popc(m));
+                pos = __shfl_sync(FULL_MASK, pos, leader);
+                if (has) tchanges[pos + __popc(m & ((1u << lane) - 1u))] = code;
+            }
         }
+        __syncthreads();
+        if (tid == 0) a.tile_nch[t] = nch;
         if (STATS && sg.stats) block_flush4(nS, nI, nR, eS, sg.stats + 4 * (int64_t)a.r, red);
+        __syncthreads(); // nch is reset for the next tile only after every read
     }
 }
 
@@ -341,32 +474,36 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_scatter_kernel(SgTic
     __shared__ int32_t hubq[SG_SIR_THREADS];
     __shared__ int32_t hubn;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int32_t n = a.nchanges[a.r];
-    for (int32_t base = blockIdx.x * SG_SIR_THREADS; base < n; base += gridDim.x * SG_SIR_THREADS) {
-        if (tid == 0) hubn = 0;
-        __syncthreads();
-        const int32_t q = base + tid;
-        if (q < n) {
-            const int32_t c = a.changes[q];
-            const int32_t g = c >= 0 ? c : ~c;
-            const int32_t delta = c >= 0 ? 1 : -1;
-            const int32_t b = a.toff[g], e = a.toff[g + 1];
-            if (e - b > 32) {
-                hubq[atomicAdd(&hubn, 1)] = c;
-            } else {
-                for (int32_t k = b; k < e; ++k) atomicAdd(a.cnt + a.tidx[k], delta);
+    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+        const int32_t n = a.tile_nch[t];
+        if (n == 0) continue; // uniform over the block
+        const int32_t *tchanges = a.changes + a.tiles[t].begin;
+        for (int32_t q0 = 0; q0 < n; q0 += SG_SIR_THREADS) {
+            if (tid == 0) hubn = 0;
+            __syncthreads();
+            const int32_t q = q0 + tid;
+            if (q < n) {
+                const int32_t c = tchanges[q];
+                const int32_t g = c >= 0 ? c : ~c;
+                const int32_t delta = c >= 0 ? 1 : -1;
+                const int32_t b = a.toff[g], e = a.toff[g + 1];
+                if (e - b > kThreadRow) {
+                    hubq[atomicAdd(&hubn, 1)] = c;
+                } else {
+                    for (int32_t k = b; k < e; ++k) atomicAdd(a.cnt + __ldg(a.tidx + k), delta);
+                }
             }
+            __syncthreads();
+            const int nh = hubn;
+            for (int h = warp; h < nh; h += kWarps) {
+                const int32_t c = hubq[h];
+                const int32_t g = c >= 0 ? c : ~c;
+                const int32_t delta = c >= 0 ? 1 : -1;
+                const int32_t b = a.toff[g], e = a.toff[g + 1];
+                for (int32_t k = b + lane; k < e; k += 32) atomicAdd(a.cnt + __ldg(a.tidx + k), delta);
+            }
+            __syncthreads();
         }
-        __syncthreads();
-        const int nh = hubn;
-        for (int h = warp; h < nh; h += kWarps) {
-            const int32_t c = hubq[h];
-            const int32_t g = c >= 0 ? c : ~c;
-            const int32_t delta = c >= 0 ? 1 : -1;
-            const int32_t b = a.toff[g], e = a.toff[g + 1];
-            for (int32_t k = b + lane; k < e; k += 32) atomicAdd(a.cnt + a.tidx[k], delta);
-        }
-        __syncthreads();
     }
 }
 
@@ -469,20 +606,24 @@ cudaError_t sg_launch_sir_count_init(const SgTickArgs &a, int grid, cudaStream_t
     return cudaGetLastError();
 }
 
-cudaError_t sg_launch_sir_count_step(const SgTickArgs &a, int variant, bool stats, int grid,
-                                     cudaStream_t st)
+cudaError_t sg_launch_sir_count_step(const SgTickArgs &a, int variant, bool stats, bool inplace,
+                                     int grid, cudaStream_t st)
 {
+#define SG_CS(V, S, P) sir_count_step_kernel<V, S, P><<<grid, SG_SIR_THREADS, 0, st>>>(a)
     if (variant == 1) {
-        if (stats)
-            sir_count_step_kernel<1, true><<<grid, SG_SIR_THREADS, 0, st>>>(a);
-        else
-            sir_count_step_kernel<1, false><<<grid, SG_SIR_THREADS, 0, st>>>(a);
+        if (stats) {
+            if (inplace) SG_CS(1, true, true); else SG_CS(1, true, false);
+        } else {
+            if (inplace) SG_CS(1, false, true); else SG_CS(1, false, false);
+        }
     } else {
-        if (stats)
-            sir_count_step_kernel<2, true><<<grid, SG_SIR_THREADS, 0, st>>>(a);
-        else
-            sir_count_step_kernel<2, false><<<grid, SG_SIR_THREADS, 0, st>>>(a);
+        if (stats) {
+            if (inplace) SG_CS(2, true, true); else SG_CS(2, true, false);
+        } else {
+            if (inplace) SG_CS(2, false, true); else SG_CS(2, false, false);
+        }
     }
+#undef SG_CS
     return cudaGetLastError();
 }
 

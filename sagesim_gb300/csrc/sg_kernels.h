@@ -44,8 +44,9 @@ struct SgTickArgs {
     int32_t hub_deg;        // pull: rows longer than this go warp-per-agent
     // count strategy
     int32_t *cnt;           // infected-neighbour count per agent
-    int32_t *changes;       // change list: agent index, ~agent for I->R
-    int32_t *nchanges;      // [ticks] counters, slot r
+    int32_t *changes;       // change list: agent index, ~agent for I->R; tile t
+                            // owns changes[tile.begin .. tile.begin + tile_nch[t])
+    int32_t *tile_nch;      // [ntiles] changes recorded by each tile this tick
     const int32_t *toff;    // transpose CSR (in-neighbours)
     const int32_t *tidx;
 };
@@ -57,8 +58,11 @@ struct SgTickArgs {
 cudaError_t sg_launch_sir_pull(const SgTickArgs &a, int variant, bool stats, int grid,
                                cudaStream_t st);
 cudaError_t sg_launch_sir_count_init(const SgTickArgs &a, int grid, cudaStream_t st);
-cudaError_t sg_launch_sir_count_step(const SgTickArgs &a, int variant, bool stats, int grid,
-                                     cudaStream_t st);
+// inplace: the state buffer is read and written in place (buf0); only changed
+// agents are stored. Valid when the count step is the engine's only step, since
+// it reads nothing but the agent's own state and count.
+cudaError_t sg_launch_sir_count_step(const SgTickArgs &a, int variant, bool stats, bool inplace,
+                                     int grid, cudaStream_t st);
 cudaError_t sg_launch_sir_count_scatter(const SgTickArgs &a, int grid, cudaStream_t st);
 cudaError_t sg_launch_opinion(const SgTickArgs &a, int grid, cudaStream_t st);
 // Copies [begin, end) of `words` 32-bit words from src to dst (write-back of
