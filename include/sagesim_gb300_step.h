@@ -38,7 +38,7 @@ typedef struct sg_step_args {
     long long tick0;         /* absolute tick at r == 0                         */
     unsigned int key;        /* seed mod 2^32                                   */
     int nprops;
-    const long long *lids;   /* RNG key per agent, NULL = agent index           */
+    const unsigned int *lids; /* RNG key (lid mod 2^32) per agent, NULL = index  */
     const int *off;          /* CSR offsets                                     */
     const int *idx;          /* CSR indices                                     */
     const double *g;         /* globals                                         */
@@ -52,7 +52,7 @@ struct sg_ctx {
     unsigned int key;
     unsigned int c0b;
     int r;
-    const long long *lids;
+    const unsigned int *lids;
     const int *off;
     const int *idx;
     const double *g;
@@ -91,7 +91,7 @@ struct sg_ctx {
     __device__ __forceinline__ int neighbor(int i, int k) const { return idx[off[i] + k]; }
     __device__ __forceinline__ unsigned int lid(int i) const
     {
-        return lids ? (unsigned int)(unsigned long long)lids[i] : (unsigned int)i;
+        return lids ? lids[i] : (unsigned int)i;
     }
     /* sagesim/math_utils.py:106-189 */
     __device__ __forceinline__ double rand_uniform(int i, long long salt) const

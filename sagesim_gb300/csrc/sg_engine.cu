@@ -21,6 +21,8 @@
 
 namespace {
 thread_local std::string g_create_error;
+// Rows longer than this are scanned by a whole block (see sg_kernels.cu).
+constexpr int32_t kMegaRow = 2048;
 }
 
 struct SgProp {
@@ -43,8 +45,8 @@ struct SgStep {
     std::vector<int32_t> written;
     SgCompiledStep *compiled = nullptr;
     // device tables
-    SgDev seg, tiles;
-    int32_t ntiles = 0;
+    SgDev seg, tiles, mega;
+    int32_t ntiles = 0, nmega = 0;
     SgSeg host_seg{};
 };
 
@@ -59,6 +61,7 @@ struct sg_engine {
     int32_t graph_flags = 0;
     SgDev off, idx, toff, tidx;
     bool have_transpose = false;
+    std::vector<int32_t> mega_agents; // agents whose row is longer than kMegaRow
     SgDev lids;
     bool has_lids = false;
     int64_t seed = 0;
@@ -216,6 +219,10 @@ int sg_set_graph_csr(sg_engine *e, const int32_t *offsets, int64_t n, const int3
     if (nnz > 0)
         SG_CK(cudaMemcpyAsync(e->idx.p, indices, (size_t)nnz * 4, cudaMemcpyHostToDevice, e->stream));
     SG_CK(cudaStreamSynchronize(e->stream));
+    e->mega_agents.clear();
+    for (int64_t i = 0; i < n; ++i)
+        if (offsets[i + 1] - offsets[i] > kMegaRow) e->mega_agents.push_back((int32_t)i);
+    for (auto &st : e->steps) st->ntiles = 0; // tile and mega tables are rebuilt
     e->n = n;
     e->nnz = nnz;
     e->graph_flags = flags;
@@ -235,8 +242,12 @@ int sg_set_logical_ids(sg_engine *e, const int64_t *lids, int64_t n)
         e->version++;
         return SG_OK;
     }
-    SG_CK(e->lids.reserve((size_t)std::max<int64_t>(n, 1) * 8));
-    SG_CK(cudaMemcpyAsync(e->lids.p, lids, (size_t)n * 8, cudaMemcpyHostToDevice, e->stream));
+    // Philox keys on lid mod 2^32 (sagesim/math_utils.py:108), so 4 bytes per
+    // agent carry the whole key.
+    std::vector<uint32_t> k32((size_t)n);
+    for (int64_t i = 0; i < n; ++i) k32[(size_t)i] = (uint32_t)(uint64_t)lids[i];
+    SG_CK(e->lids.reserve((size_t)std::max<int64_t>(n, 1) * 4));
+    SG_CK(cudaMemcpyAsync(e->lids.p, k32.data(), (size_t)n * 4, cudaMemcpyHostToDevice, e->stream));
     SG_CK(cudaStreamSynchronize(e->stream));
     e->has_lids = true;
     e->version++;
@@ -469,7 +480,7 @@ static int prepare_step(sg_engine *e, SgStep *s, int64_t tick0, unsigned long lo
     memset(&g, 0, sizeof g);
     g.tick0 = tick0;
     g.end_tick = std::numeric_limits<int64_t>::max();
-    g.lids = e->has_lids ? e->lids.as<int64_t>() : nullptr;
+    g.lids = e->has_lids ? e->lids.as<uint32_t>() : nullptr;
     g.lid_base = 0;
     g.key = (uint32_t)(uint64_t)e->seed;
     if (s->kind != 0) {
@@ -496,6 +507,14 @@ static int prepare_step(sg_engine *e, SgStep *s, int64_t tick0, unsigned long lo
         SG_CK(s->tiles.reserve(std::max<size_t>(tiles.size(), 1) * sizeof(SgTile)));
         if (!tiles.empty())
             SG_CK(cudaMemcpyAsync(s->tiles.p, tiles.data(), tiles.size() * sizeof(SgTile),
+                                  cudaMemcpyHostToDevice, e->stream));
+        std::vector<SgMega> mg;
+        for (int32_t a : e->mega_agents)
+            if (a >= s->begin && a < s->end) mg.push_back(SgMega{a, 0});
+        s->nmega = (int32_t)mg.size();
+        SG_CK(s->mega.reserve(std::max<size_t>(mg.size(), 1) * sizeof(SgMega)));
+        if (!mg.empty())
+            SG_CK(cudaMemcpyAsync(s->mega.p, mg.data(), mg.size() * sizeof(SgMega),
                                   cudaMemcpyHostToDevice, e->stream));
     }
     SG_CK(s->seg.reserve(sizeof(SgSeg)));
@@ -534,6 +553,10 @@ static SgTickArgs base_args(sg_engine *e, SgStep *s, int32_t r, bool inplace)
     a.ntiles = s->ntiles;
     a.r = r;
     a.hub_deg = e->hub_deg;
+    a.mega = s->mega.as<SgMega>();
+    a.nmega = s->nmega;
+    a.mega_blocks = std::min(s->nmega, e->sm_count);
+    a.mega_row = kMegaRow;
     a.cnt = e->cnt.as<int32_t>();
     a.changes = e->changes.as<int32_t>();
     a.tile_nch = e->tile_nch.as<int32_t>();
@@ -567,7 +590,8 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
     if (pl.count_step) {
         SgStep *s = pl.count_step;
         SgTickArgs a = base_args(e, s, 0, pl.count_inplace);
-        SG_PROF_LAUNCH("sir_count_init", sg_launch_sir_count_init(a, grid_for(e, s->ntiles), e->stream));
+        SG_PROF_LAUNCH("sir_count_init",
+                       sg_launch_sir_count_init(a, grid_for(e, s->ntiles) + a.mega_blocks, e->stream));
     }
     for (int32_t r = 0; r < nticks; ++r) {
         for (int32_t p : pl.copy_props) {
@@ -587,7 +611,8 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
                     SG_PROF_LAUNCH("sir_count_step", sg_launch_sir_count_step(a, variant, stats_on, inplace, grid, e->stream));
                     SG_PROF_LAUNCH("sir_count_scatter", sg_launch_sir_count_scatter(a, grid_sc, e->stream));
                 } else {
-                    SG_PROF_LAUNCH("sir_pull", sg_launch_sir_pull(a, variant, stats_on, grid, e->stream));
+                    SG_PROF_LAUNCH("sir_pull",
+                                   sg_launch_sir_pull(a, variant, stats_on, grid + a.mega_blocks, e->stream));
                 }
             } else if (s->kind == SG_BUILTIN_OPINION) {
                 SG_PROF_LAUNCH("opinion", sg_launch_opinion(a, grid, e->stream));
@@ -599,7 +624,7 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
                 L.tick0 = s->host_seg.tick0;
                 L.key = s->host_seg.key;
                 L.nprops = (int)e->props.size();
-                L.lids = (const long long *)(e->has_lids ? e->lids.p : nullptr);
+                L.lids = (const unsigned int *)(e->has_lids ? e->lids.p : nullptr);
                 L.off = e->off.as<int32_t>();
                 L.idx = e->idx.as<int32_t>();
                 L.g = e->globals_dev.as<double>();

@@ -62,7 +62,7 @@ __device__ __forceinline__ void block_flush4(unsigned long long v0, unsigned lon
 
 __device__ __forceinline__ uint32_t seg_lid(const SgSeg &sg, int32_t i)
 {
-    return sg.lids ? (uint32_t)(uint64_t)sg.lids[i] : (uint32_t)(i - sg.lid_base);
+    return sg.lids ? __ldg(sg.lids + i) : (uint32_t)(i - sg.lid_base);
 }
 
 // ---- neighbour scans ------------------------------------------------------------
@@ -72,12 +72,13 @@ __device__ __forceinline__ uint32_t seg_lid(const SgSeg &sg, int32_t i)
 // in batches whose loads are all independent (memory-level parallelism), and
 // the draws for a batch's c infected neighbours are tested together.
 //
-// Three bins by row length: a thread scans rows of <= kThreadRow entries
-// (4 independent gathers per step), a warp scans rows of <= kWarpRow entries
-// (128 per step), the whole block scans longer rows (1024 per step).
+// Three bins by row length, all warp-synchronous: a lane scans its own row
+// when it has <= kThreadRow entries (4 independent gathers per step); the
+// whole warp scans rows of <= kWarpRow entries (128 per step); rows longer
+// than that ("mega" rows, a few dozen in a 10^7-agent power-law graph) are
+// listed at setup and scanned by dedicated blocks (1024 entries per step).
 constexpr int kBatch = 4;
 constexpr int32_t kThreadRow = 32;
-constexpr int32_t kWarpRow = 2048;
 
 // Number of infected entries among row[k .. min(k+4, e)), e > k.
 __device__ __forceinline__ int batch_count(const int32_t *__restrict__ idx,
@@ -94,7 +95,7 @@ __device__ __forceinline__ int batch_count(const int32_t *__restrict__ idx,
     return (s0 == ci) + (k + 1 < e && s1 == ci) + (k + 2 < e && s2 == ci) + (k + 3 < e && s3 == ci);
 }
 
-// SIR-B outcome for one agent from its row, thread path.
+// SIR-B outcome for one agent from its row, lane path.
 __device__ __forceinline__ bool trials_thread(const int32_t *__restrict__ idx,
                                               const int32_t *__restrict__ sin, int32_t b,
                                               int32_t e, int32_t ci, uint32_t c0b, uint32_t lid,
@@ -141,8 +142,7 @@ __device__ __forceinline__ int warp_batch_count(const int32_t *__restrict__ idx,
     const int32_t n3 = __ldg(idx + min(k + 96, last));
     const int32_t s0 = __ldg(sin + n0), s1 = __ldg(sin + n1), s2 = __ldg(sin + n2),
                   s3 = __ldg(sin + n3);
-    const int mine = (v0 && s0 == ci) + (v1 && s1 == ci) + (v2 && s2 == ci) + (v3 && s3 == ci);
-    int c = mine;
+    int c = (v0 && s0 == ci) + (v1 && s1 == ci) + (v2 && s2 == ci) + (v3 && s3 == ci);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(FULL_MASK, c, o);
     return c;
@@ -180,8 +180,9 @@ __device__ __forceinline__ bool warp_row(const int32_t *__restrict__ idx,
     return false;
 }
 
-// Block path for the longest rows: 256 threads x 4 entries per step; the
-// result is broadcast through __syncthreads_or / a shared counter.
+// Block path for mega rows: 256 threads x 4 entries per step; the result is
+// broadcast through __syncthreads_or / a shared counter. Called by every
+// thread of the block.
 template <int VARIANT>
 __device__ __forceinline__ bool block_row(const int32_t *__restrict__ idx,
                                           const int32_t *__restrict__ sin, int32_t b, int32_t e,
@@ -189,6 +190,7 @@ __device__ __forceinline__ bool block_row(const int32_t *__restrict__ idx,
                                           uint32_t kinf, int32_t *sh_count, int32_t *count)
 {
     const int tid = threadIdx.x;
+    __syncthreads(); // previous users of *sh_count are done
     if (tid == 0) *sh_count = 0;
     __syncthreads();
     for (int32_t k0 = b; k0 < e; k0 += 4 * SG_SIR_THREADS) {
@@ -216,37 +218,54 @@ __device__ __forceinline__ bool block_row(const int32_t *__restrict__ idx,
             ok = sg_philox_k23(c0b + 2u + (uint32_t)q, lid, key) < kinf;
         return __syncthreads_or(ok) != 0;
     }
-    __syncthreads();
     return false;
 }
 
-// Shared-memory queues of deferred rows for one 256-agent chunk.
-struct HubQueues {
-    int32_t warpq[SG_SIR_THREADS];
-    int32_t blockq[SG_SIR_THREADS];
-    int32_t nwarp, nblock;
-    int32_t count;
-};
-
-__device__ __forceinline__ void defer_row(HubQueues &q, int32_t i, int32_t deg)
-{
-    if (deg > kWarpRow)
-        q.blockq[atomicAdd(&q.nblock, 1)] = i;
-    else
-        q.warpq[atomicAdd(&q.nwarp, 1)] = i;
-}
-
 // ---- pull strategy --------------------------------------------------------------
+// Blocks [0, gridDim.x - a.mega_blocks) walk the tiles, one warp per 32
+// consecutive agents; the last a.mega_blocks blocks each take mega rows.
 template <int VARIANT, bool STATS>
 __global__ void __launch_bounds__(SG_SIR_THREADS) sir_pull_kernel(SgTickArgs a)
 {
-    __shared__ HubQueues hq;
     __shared__ unsigned long long red[4][kWarps];
+    __shared__ int32_t sh_count;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int32_t *__restrict__ off = a.off;
     const int32_t *__restrict__ idx = a.idx;
+    const int tile_blocks = (int)gridDim.x - a.mega_blocks;
 
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+    if ((int)blockIdx.x >= tile_blocks) {
+        for (int q = (int)blockIdx.x - tile_blocks; q < a.nmega; q += a.mega_blocks) {
+            const SgMega mg = a.mega[q];
+            const SgSeg &sg = a.segs[mg.seg];
+            const int64_t tick = sg.tick0 + a.r;
+            if (tick >= sg.end_tick) continue;
+            const int par = (sg.par0 + a.r) & 1;
+            const int32_t *__restrict__ sin = (const int32_t *)(par ? a.buf1 : a.buf0);
+            int32_t *__restrict__ sout = (int32_t *)(par ? a.buf0 : a.buf1);
+            const int32_t h = mg.agent;
+            if (sin[h] != sg.cs) continue; // handled by the tile pass
+            const uint32_t c0b = sg_c0base(tick);
+            const uint32_t lid = seg_lid(sg, h);
+            bool lucky = true;
+            if (VARIANT == 1) lucky = sg_philox_k23(c0b + 1u, lid, sg.key) < sg.kinf;
+            bool inf = false;
+            if (lucky)
+                inf = block_row<VARIANT>(idx, sin, __ldg(off + h), __ldg(off + h + 1), sg.ci, c0b,
+                                         lid, sg.key, sg.kinf, &sh_count, nullptr);
+            if (tid == 0) {
+                sout[h] = inf ? sg.ci : sg.cs;
+                if (STATS && sg.stats) {
+                    atomicAdd(sg.stats + 4 * (int64_t)a.r + (inf ? 1 : 0), 1ull);
+                    atomicAdd(sg.stats + 4 * (int64_t)a.r + 3,
+                              (unsigned long long)(__ldg(off + h + 1) - __ldg(off + h)));
+                }
+            }
+        }
+        return;
+    }
+
+    for (int t = blockIdx.x; t < a.ntiles; t += tile_blocks) {
         const SgTile tile = a.tiles[t];
         const SgSeg &sg = a.segs[tile.seg];
         const int64_t tick = sg.tick0 + a.r;
@@ -257,76 +276,59 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_pull_kernel(SgTickArgs a)
         const uint32_t c0b = sg_c0base(tick);
         const uint32_t key = sg.key, kinf = sg.kinf, krec = sg.krec;
         const int32_t cs = sg.cs, ci = sg.ci, cr = sg.cr;
+        const int32_t mega_row = a.mega_row;
         unsigned long long nS = 0, nI = 0, nR = 0, eS = 0;
 
-        for (int32_t base = tile.begin; base < tile.end; base += SG_SIR_THREADS) {
-            if (tid == 0) {
-                hq.nwarp = 0;
-                hq.nblock = 0;
-            }
-            __syncthreads();
-            const int32_t i = base + tid;
-            if (i < tile.end) {
-                const int32_t s = sin[i];
-                int32_t out = s;
-                bool deferred = false;
-                if (s == ci) {
-                    if (sg_philox_k23(c0b + 1u, seg_lid(sg, i), key) < krec) out = cr;
-                } else if (s == cs) {
-                    const uint32_t lid = seg_lid(sg, i);
-                    const bool lucky = VARIANT == 2 || sg_philox_k23(c0b + 1u, lid, key) < kinf;
-                    if (lucky || STATS) {
-                        const int32_t b = __ldg(off + i), e = __ldg(off + i + 1);
+        for (int32_t wbase = tile.begin + warp * 32; wbase < tile.end; wbase += SG_SIR_THREADS) {
+            const int32_t i = wbase + lane;
+            const bool valid = i < tile.end;
+            const int32_t s = valid ? sin[i] : INT32_MIN;
+            int32_t out = s;
+            bool medium = false, skip = false;
+            int32_t b = 0, e = 0;
+            uint32_t lid = 0;
+            if (s == ci) {
+                if (sg_philox_k23(c0b + 1u, seg_lid(sg, i), key) < krec) out = cr;
+            } else if (s == cs) {
+                lid = seg_lid(sg, i);
+                const bool lucky = VARIANT == 2 || sg_philox_k23(c0b + 1u, lid, key) < kinf;
+                if (lucky || STATS) {
+                    b = __ldg(off + i);
+                    e = __ldg(off + i + 1);
+                    if (e - b > mega_row) {
+                        skip = true; // a mega block writes this agent
+                    } else {
                         if (STATS) eS += (unsigned long long)(e - b);
                         if (lucky) {
-                            if (e - b > kThreadRow) {
-                                deferred = true;
-                                defer_row(hq, i, e - b);
-                            } else if (VARIANT == 1 ? any_infected_thread(idx, sin, b, e, ci)
-                                                    : trials_thread(idx, sin, b, e, ci, c0b, lid,
-                                                                    key, kinf)) {
+                            if (e - b > kThreadRow)
+                                medium = true;
+                            else if (VARIANT == 1 ? any_infected_thread(idx, sin, b, e, ci)
+                                                  : trials_thread(idx, sin, b, e, ci, c0b, lid, key,
+                                                                  kinf))
                                 out = ci;
-                            }
                         }
                     }
                 }
-                if (!deferred) {
-                    sout[i] = out;
-                    if (STATS) {
-                        nS += (out == cs);
-                        nI += (out == ci);
-                        nR += (out == cr);
-                    }
+            }
+            unsigned m = __ballot_sync(FULL_MASK, medium);
+            while (m) {
+                const int l = __ffs(m) - 1;
+                m &= m - 1;
+                const int32_t hb = __shfl_sync(FULL_MASK, b, l);
+                const int32_t he = __shfl_sync(FULL_MASK, e, l);
+                const uint32_t hl = __shfl_sync(FULL_MASK, lid, l);
+                const bool inf = warp_row<VARIANT>(idx, sin, hb, he, ci, c0b, hl, key, kinf, lane,
+                                                   nullptr);
+                if (lane == l && inf) out = ci;
+            }
+            if (valid && !skip) {
+                sout[i] = out;
+                if (STATS) {
+                    nS += (out == cs);
+                    nI += (out == ci);
+                    nR += (out == cr);
                 }
             }
-            __syncthreads();
-            const int nw = hq.nwarp, nb = hq.nblock;
-            for (int q = warp; q < nw; q += kWarps) {
-                const int32_t h = hq.warpq[q];
-                const bool inf = warp_row<VARIANT>(idx, sin, __ldg(off + h), __ldg(off + h + 1), ci,
-                                                   c0b, seg_lid(sg, h), key, kinf, lane, nullptr);
-                if (lane == 0) {
-                    sout[h] = inf ? ci : cs;
-                    if (STATS) {
-                        nS += !inf;
-                        nI += inf;
-                    }
-                }
-            }
-            for (int q = 0; q < nb; ++q) {
-                const int32_t h = hq.blockq[q];
-                const bool inf = block_row<VARIANT>(idx, sin, __ldg(off + h), __ldg(off + h + 1), ci,
-                                                    c0b, seg_lid(sg, h), key, kinf, &hq.count,
-                                                    nullptr);
-                if (tid == 0) {
-                    sout[h] = inf ? ci : cs;
-                    if (STATS) {
-                        nS += !inf;
-                        nI += inf;
-                    }
-                }
-            }
-            __syncthreads();
         }
         if (STATS && sg.stats) block_flush4(nS, nI, nR, eS, sg.stats + 4 * (int64_t)a.r, red);
     }
@@ -343,46 +345,57 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_pull_kernel(SgTickArgs a)
 
 __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_init_kernel(SgTickArgs a)
 {
-    __shared__ HubQueues hq;
+    __shared__ int32_t sh_count;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+    const int tile_blocks = (int)gridDim.x - a.mega_blocks;
+    if ((int)blockIdx.x >= tile_blocks) {
+        for (int q = (int)blockIdx.x - tile_blocks; q < a.nmega; q += a.mega_blocks) {
+            const SgMega mg = a.mega[q];
+            const SgSeg &sg = a.segs[mg.seg];
+            const int32_t *__restrict__ sin = (const int32_t *)((sg.par0 & 1) ? a.buf1 : a.buf0);
+            const int32_t h = mg.agent;
+            if (sin[h] != sg.cs) continue;
+            int32_t c = 0;
+            block_row<0>(a.idx, sin, a.off[h], a.off[h + 1], sg.ci, 0, 0, 0, 0, &sh_count, &c);
+            if (tid == 0) a.cnt[h] = c;
+        }
+        return;
+    }
+    for (int t = blockIdx.x; t < a.ntiles; t += tile_blocks) {
         const SgTile tile = a.tiles[t];
         const SgSeg &sg = a.segs[tile.seg];
-        const int par = sg.par0 & 1;
-        const int32_t *__restrict__ sin = (const int32_t *)(par ? a.buf1 : a.buf0);
+        const int32_t *__restrict__ sin = (const int32_t *)((sg.par0 & 1) ? a.buf1 : a.buf0);
         const int32_t ci = sg.ci, cs = sg.cs;
-        for (int32_t base = tile.begin; base < tile.end; base += SG_SIR_THREADS) {
-            if (tid == 0) {
-                hq.nwarp = 0;
-                hq.nblock = 0;
-            }
-            __syncthreads();
-            const int32_t i = base + tid;
+        for (int32_t wbase = tile.begin + warp * 32; wbase < tile.end; wbase += SG_SIR_THREADS) {
+            const int32_t i = wbase + lane;
+            bool medium = false;
+            int32_t b = 0, e = 0;
             if (i < tile.end && sin[i] == cs) {
-                const int32_t b = a.off[i], e = a.off[i + 1];
-                if (e - b > kThreadRow)
-                    defer_row(hq, i, e - b);
-                else
+                b = a.off[i];
+                e = a.off[i + 1];
+                if (e - b > a.mega_row) {
+                    // mega block
+                } else if (e - b > kThreadRow) {
+                    medium = true;
+                } else {
                     a.cnt[i] = count_thread(a.idx, sin, b, e, ci);
+                }
             }
-            __syncthreads();
-            const int nw = hq.nwarp, nb = hq.nblock;
-            for (int q = warp; q < nw; q += kWarps) {
-                const int32_t h = hq.warpq[q];
+            unsigned m = __ballot_sync(FULL_MASK, medium);
+            while (m) {
+                const int l = __ffs(m) - 1;
+                m &= m - 1;
+                const int32_t hb = __shfl_sync(FULL_MASK, b, l);
+                const int32_t he = __shfl_sync(FULL_MASK, e, l);
                 int32_t c = 0;
-                warp_row<0>(a.idx, sin, a.off[h], a.off[h + 1], ci, 0, 0, 0, 0, lane, &c);
-                if (lane == 0) a.cnt[h] = c;
+                warp_row<0>(a.idx, sin, hb, he, ci, 0, 0, 0, 0, lane, &c);
+                if (lane == l) a.cnt[i] = c;
             }
-            for (int q = 0; q < nb; ++q) {
-                const int32_t h = hq.blockq[q];
-                int32_t c = 0;
-                block_row<0>(a.idx, sin, a.off[h], a.off[h + 1], ci, 0, 0, 0, 0, &hq.count, &c);
-                if (tid == 0) a.cnt[h] = c;
-            }
-            __syncthreads();
         }
     }
 }
+
+constexpr int kPerThread = SG_TILE / SG_SIR_THREADS; // agents per thread in a tile
 
 template <int VARIANT, bool STATS, bool INPLACE>
 __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickArgs a)
@@ -408,46 +421,58 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickAr
         unsigned long long nS = 0, nI = 0, nR = 0, eS = 0;
         if (tid == 0) nch = 0;
         __syncthreads();
-        // every thread runs the same number of iterations: the ballot below
-        // needs all 32 lanes
-        for (int32_t base = tile.begin; base < tile.end; base += SG_SIR_THREADS) {
-            const int32_t i = base + tid;
+        // all loads of the thread's agents are issued before any is used
+        int32_t s[kPerThread], k[kPerThread];
+        uint32_t lid[kPerThread];
+#pragma unroll
+        for (int q = 0; q < kPerThread; ++q) {
+            const int32_t i = tile.begin + q * SG_SIR_THREADS + tid;
+            s[q] = i < tile.end ? sin[i] : INT32_MIN;
+        }
+#pragma unroll
+        for (int q = 0; q < kPerThread; ++q) {
+            const int32_t i = tile.begin + q * SG_SIR_THREADS + tid;
+            k[q] = s[q] == cs ? a.cnt[i] : 0;
+        }
+#pragma unroll
+        for (int q = 0; q < kPerThread; ++q) {
+            const int32_t i = tile.begin + q * SG_SIR_THREADS + tid;
+            lid[q] = (s[q] == ci || k[q] > 0) ? seg_lid(sg, i) : 0u;
+        }
+#pragma unroll
+        for (int q = 0; q < kPerThread; ++q) {
+            const int32_t i = tile.begin + q * SG_SIR_THREADS + tid;
+            int32_t out = s[q];
             bool has = false;
             int32_t code = 0;
-            if (i < tile.end) {
-                const int32_t s = sin[i];
-                int32_t out = s;
-                if (s == ci) {
-                    if (sg_philox_k23(c0b + 1u, seg_lid(sg, i), key) < krec) {
-                        out = cr;
-                        has = true;
-                        code = ~i;
-                    }
-                } else if (s == cs) {
-                    if (STATS) eS += (unsigned long long)(__ldg(a.off + i + 1) - __ldg(a.off + i));
-                    const int32_t k = a.cnt[i];
-                    if (k > 0) {
-                        const uint32_t lid = seg_lid(sg, i);
-                        bool inf = false;
-                        if (VARIANT == 1) {
-                            inf = sg_philox_k23(c0b + 1u, lid, key) < kinf;
-                        } else {
-                            for (int32_t j = 0; j < k; ++j) {
-                                if (sg_philox_k23(c0b + 2u + (uint32_t)j, lid, key) < kinf) {
-                                    inf = true;
-                                    break;
-                                }
-                            }
-                        }
-                        if (inf) {
-                            out = ci;
-                            has = true;
-                            code = i;
+            if (s[q] == ci) {
+                if (sg_philox_k23(c0b + 1u, lid[q], key) < krec) {
+                    out = cr;
+                    has = true;
+                    code = ~i;
+                }
+            } else if (k[q] > 0) {
+                bool inf = false;
+                if (VARIANT == 1) {
+                    inf = sg_philox_k23(c0b + 1u, lid[q], key) < kinf;
+                } else {
+                    for (int32_t j = 0; j < k[q]; ++j) {
+                        if (sg_philox_k23(c0b + 2u + (uint32_t)j, lid[q], key) < kinf) {
+                            inf = true;
+                            break;
                         }
                     }
                 }
+                if (inf) {
+                    out = ci;
+                    has = true;
+                    code = i;
+                }
+            }
+            if (i < tile.end) {
                 if (!INPLACE || has) sout[i] = out;
                 if (STATS) {
+                    if (s[q] == cs) eS += (unsigned long long)(__ldg(a.off + i + 1) - __ldg(a.off + i));
                     nS += (out == cs);
                     nI += (out == ci);
                     nR += (out == cr);
@@ -469,40 +494,49 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickAr
     }
 }
 
+// Warp-synchronous: each warp takes 32 changes of a tile; short transpose rows
+// are updated by their lane, longer ones by the whole warp.
 __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_scatter_kernel(SgTickArgs a)
 {
-    __shared__ int32_t hubq[SG_SIR_THREADS];
-    __shared__ int32_t hubn;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
         const int32_t n = a.tile_nch[t];
-        if (n == 0) continue; // uniform over the block
+        if (n == 0) continue;
         const int32_t *tchanges = a.changes + a.tiles[t].begin;
-        for (int32_t q0 = 0; q0 < n; q0 += SG_SIR_THREADS) {
-            if (tid == 0) hubn = 0;
-            __syncthreads();
-            const int32_t q = q0 + tid;
-            if (q < n) {
-                const int32_t c = tchanges[q];
-                const int32_t g = c >= 0 ? c : ~c;
-                const int32_t delta = c >= 0 ? 1 : -1;
-                const int32_t b = a.toff[g], e = a.toff[g + 1];
-                if (e - b > kThreadRow) {
-                    hubq[atomicAdd(&hubn, 1)] = c;
-                } else {
-                    for (int32_t k = b; k < e; ++k) atomicAdd(a.cnt + __ldg(a.tidx + k), delta);
+        for (int32_t q0 = warp * 32; q0 < n; q0 += SG_SIR_THREADS) {
+            const int32_t q = q0 + lane;
+            const bool valid = q < n;
+            const int32_t c = valid ? tchanges[q] : 0;
+            const int32_t g = c >= 0 ? c : ~c;
+            const int32_t delta = c >= 0 ? 1 : -1;
+            int32_t b = 0, e = 0;
+            if (valid) {
+                b = __ldg(a.toff + g);
+                e = __ldg(a.toff + g + 1);
+            }
+            const bool long_row = e - b > kThreadRow;
+            if (!long_row) {
+                for (int32_t k = b; k < e; k += 4) {
+                    const int32_t last = e - 1;
+                    const int32_t d0 = __ldg(a.tidx + k);
+                    const int32_t d1 = __ldg(a.tidx + min(k + 1, last));
+                    const int32_t d2 = __ldg(a.tidx + min(k + 2, last));
+                    const int32_t d3 = __ldg(a.tidx + min(k + 3, last));
+                    atomicAdd(a.cnt + d0, delta);
+                    if (k + 1 < e) atomicAdd(a.cnt + d1, delta);
+                    if (k + 2 < e) atomicAdd(a.cnt + d2, delta);
+                    if (k + 3 < e) atomicAdd(a.cnt + d3, delta);
                 }
             }
-            __syncthreads();
-            const int nh = hubn;
-            for (int h = warp; h < nh; h += kWarps) {
-                const int32_t c = hubq[h];
-                const int32_t g = c >= 0 ? c : ~c;
-                const int32_t delta = c >= 0 ? 1 : -1;
-                const int32_t b = a.toff[g], e = a.toff[g + 1];
-                for (int32_t k = b + lane; k < e; k += 32) atomicAdd(a.cnt + __ldg(a.tidx + k), delta);
+            unsigned m = __ballot_sync(FULL_MASK, long_row);
+            while (m) {
+                const int l = __ffs(m) - 1;
+                m &= m - 1;
+                const int32_t hb = __shfl_sync(FULL_MASK, b, l);
+                const int32_t he = __shfl_sync(FULL_MASK, e, l);
+                const int32_t hd = __shfl_sync(FULL_MASK, delta, l);
+                for (int32_t k = hb + lane; k < he; k += 32) atomicAdd(a.cnt + __ldg(a.tidx + k), hd);
             }
-            __syncthreads();
         }
     }
 }

@@ -16,7 +16,7 @@
 struct SgSeg {
     int64_t tick0;          // segment's absolute tick at r == 0
     int64_t end_tick;       // the segment does no work at ticks >= end_tick
-    const int64_t *lids;    // RNG key per (global) agent index; NULL -> i - lid_base
+    const uint32_t *lids;   // RNG key (lid mod 2^32) per global agent index; NULL -> i - lid_base
     int32_t lid_base;       // global index of the segment's first agent
     int32_t variant;        // 1 = SIR-A, 2 = SIR-B, 3 = opinion
     uint32_t key;           // seed mod 2^32
@@ -33,6 +33,12 @@ struct SgTile {
     int32_t seg, begin, end, pad;
 };
 
+// An agent whose CSR row is longer than SgTickArgs::mega_row; scanned by a
+// whole block (listed once per graph).
+struct SgMega {
+    int32_t agent, seg;
+};
+
 struct SgTickArgs {
     const int32_t *off;     // CSR offsets (global agent index)
     const int32_t *idx;     // CSR indices (global agent index)
@@ -41,7 +47,11 @@ struct SgTickArgs {
     const SgTile *tiles;
     int32_t ntiles;
     int32_t r;              // tick relative to the run start
-    int32_t hub_deg;        // pull: rows longer than this go warp-per-agent
+    int32_t hub_deg;        // unused (rows <= 32 are lane-scanned, longer warp-scanned)
+    const SgMega *mega;     // rows longer than mega_row, scanned by whole blocks
+    int32_t nmega;
+    int32_t mega_blocks;    // the last mega_blocks blocks of the grid take mega rows
+    int32_t mega_row;
     // count strategy
     int32_t *cnt;           // infected-neighbour count per agent
     int32_t *changes;       // change list: agent index, ~agent for I->R; tile t

@@ -1,0 +1,75 @@
+"""Step functions written in the reference's own dialect (CuPy-JIT Python).
+
+Used only by make_golden.py, which runs them through the reference's real
+Model.setup()/simulate() pipeline (AST rewrite, seed injection, double
+buffering, fused kernel) on CPU to produce golden fixtures. They are user
+model code for the reference, not part of this package.
+
+sir_per_neighbour_step: per-infected-neighbour SIR. An infected agent recovers
+  when philox(salt 1) < p_recovery. A susceptible agent scans its neighbours in
+  CSR order; the j-th infected neighbour found (j = 0, 1, ...) draws
+  philox(salt 2 + j) and the first draw below p_infection infects it.
+opinion_step: weighted mean of the first min(deg, 8) ordered neighbours'
+  opinions (float32 arithmetic in row order, normalised by the sum of |w|),
+  plus noise_sigma * rand_normal(salt 1) in float64, clamped to [0, 1].
+"""
+import cupy as cp
+from cupyx import jit
+
+from sagesim.math_utils import rand_normal, rand_uniform_philox
+
+
+@jit.rawkernel(device="cuda")
+def sir_per_neighbour_step(
+    tick, agent_index, p_infection, p_recovery,
+    agent_ids, breeds, locations, state_tensor,
+):
+    neighbor_indices = locations[agent_index]
+    agent_state = int(state_tensor[agent_index])
+    if agent_state == 2:
+        rand = rand_uniform_philox(tick, agent_index, 1)
+        if rand < p_recovery:
+            state_tensor[agent_index] = 3
+    elif agent_state == 1:
+        i = 0
+        j = 0
+        infected = False
+        while i < len(neighbor_indices) and not infected:
+            neighbor_index = int(neighbor_indices[i])
+            if int(state_tensor[neighbor_index]) == 2:
+                rand = rand_uniform_philox(tick, agent_index, 2 + j)
+                if rand < p_infection:
+                    state_tensor[agent_index] = 2
+                    infected = True
+                j += 1
+            i += 1
+
+
+@jit.rawkernel(device="cuda")
+def opinion_step(
+    tick, agent_index, noise_sigma,
+    agent_ids, breeds, locations, opinion, weights,
+):
+    neighbor_indices = locations[agent_index]
+    m = len(neighbor_indices)
+    if m > 8:
+        m = 8
+    acc = cp.float32(0.0)
+    norm = cp.float32(0.0)
+    j = 0
+    while j < m:
+        w = cp.float32(weights[agent_index][j])
+        nb = int(neighbor_indices[j])
+        acc = cp.float32(acc + cp.float32(w * cp.float32(opinion[nb])))
+        norm = cp.float32(norm + abs(w))
+        j += 1
+    x = cp.float32(opinion[agent_index])
+    if norm > 0:
+        x = cp.float32(acc / norm)
+    z = rand_normal(tick, agent_index, 1)
+    y = float(x) + noise_sigma * z
+    if y < 0.0:
+        y = 0.0
+    if y > 1.0:
+        y = 1.0
+    opinion[agent_index] = y

@@ -14,21 +14,61 @@ def _init_state(n, frac, seed, codes=(1, 2, 3)):
     return st
 
 
+def csr_from_edges(n, a, b):
+    """Symmetric CSR (duplicates kept out) from undirected edge arrays."""
+    a = np.asarray(a, dtype=np.int64)
+    b = np.asarray(b, dtype=np.int64)
+    keep = a != b
+    src = np.concatenate([a[keep], b[keep]])
+    dst = np.concatenate([b[keep], a[keep]])
+    key = np.unique(src * n + dst)
+    src, dst = key // n, key % n
+    off = np.zeros(n + 1, dtype=np.int32)
+    np.add.at(off, src + 1, 1)
+    return np.cumsum(off, dtype=np.int64).astype(np.int32), dst.astype(np.int32)
+
+
+def hub_graph(seed=3):
+    """BA graph plus three hubs of 2500-6000 neighbours: rows for every bin."""
+    n = 30000
+    off, idx = graphs.barabasi_albert(n, 3, seed)
+    src = np.repeat(np.arange(n), np.diff(off))
+    rng = np.random.default_rng(seed)
+    a, b = [src], [idx]
+    for h, deg in ((5, 6000), (17, 2500), (123, 4000)):
+        nb = rng.choice(n, size=deg, replace=False)
+        a.append(np.full(deg, h))
+        b.append(nb)
+    return csr_from_edges(n, np.concatenate(a), np.concatenate(b))
+
+
 @pytest.mark.parametrize("variant", ["A", "B"])
 @pytest.mark.parametrize("strategy", ["pull", "count"])
-@pytest.mark.parametrize("kind", ["er", "ba"])
+@pytest.mark.parametrize("kind", ["er", "ba", "hubs", "directed"])
 def test_sir_matches_oracle_every_tick(variant, strategy, kind):
     if kind == "er":
         off, idx = graphs.erdos_renyi(10000, 0.001, 0)
         beta, gamma = 0.05, 0.1
-    else:
+    elif kind == "ba":
         off, idx = graphs.barabasi_albert(20000, 4, 1)
         beta, gamma = 0.03, 0.07
+    elif kind == "hubs":
+        off, idx = hub_graph()
+        assert np.diff(off).max() > 2048
+        beta, gamma = 0.02, 0.1
+    else:  # directed: rows are out-neighbours only, the count strategy needs the transpose
+        n = 15000
+        rng = np.random.default_rng(11)
+        deg = rng.integers(0, 12, size=n)
+        deg[7] = 3000
+        off = np.concatenate([[0], np.cumsum(deg)]).astype(np.int32)
+        idx = rng.integers(0, n, size=int(off[-1])).astype(np.int32)
+        beta, gamma = 0.1, 0.05
     n = off.size - 1
     st0 = _init_state(n, 0.01, 0)
     ticks = 60
     with Engine() as e:
-        e.set_graph(off, idx, symmetric=True)
+        e.set_graph(off, idx, symmetric=(kind != "directed"))
         e.set_seed(7)
         p = e.add_property("state", np.int32, init=st0)
         e.add_sir(p, beta, gamma, variant=variant, strategy=strategy)
