@@ -184,6 +184,28 @@ int sg_profile_enable(sg_engine *e, int32_t on);
 int sg_profile_get(sg_engine *e, int32_t kind, char *name, size_t cap, int64_t *launches,
                    double *total_ms);
 
+/* ---- allocation-free SIR ticks ------------------------------------------------------
+ * No counterpart in the reference. For callers that cannot allocate device
+ * memory (their memory is owned by a pool or plan of their own, they run while
+ * a stream is captured, or their plugin contract forbids allocation): runs
+ * nticks ticks [tick0, tick0 + nticks) of SIR (builtin = SG_BUILTIN_SIR_A or
+ * SG_BUILTIN_SIR_B, count strategy) on an undirected graph given as a
+ * symmetric CSR in device memory, updating d_state (int32, device) in place,
+ * RNG key = agent index. All scratch memory comes from one static device array
+ * of SG_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until
+ * exit; the call allocates nothing. n above SG_NOALLOC_MAX_AGENTS is rejected
+ * with SG_ERR_INVALID (message via sg_last_error(NULL, ...)). The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture. Calls
+ * share the array: calls that overlap on the GPU race and give wrong results;
+ * calls on one stream are safe. Asynchronous on `stream` (NULL = legacy). */
+#define SG_NOALLOC_MAX_AGENTS 1048576
+#define SG_NOALLOC_SCRATCH_BYTES (8u * 1048576u + 16384u)
+int sg_sir_run_noalloc(const int32_t *d_offsets, const int32_t *d_indices, int32_t *d_state,
+                       int64_t n, int32_t builtin, int64_t seed, int64_t tick0, int32_t nticks,
+                       double beta, double gamma, int32_t code_s, int32_t code_i, int32_t code_r,
+                       void *stream);
+
 /* ---- host-side workload utilities (no counterpart in the reference, which
  * builds graphs with networkx and partitions with METIS:
  * sagesim/generate_partition.py:24-69, sagesim/partition_utils.py:39-103) ---- */

@@ -107,6 +107,7 @@ SIGNATURES = {
     "sg_restore": [_P],
     "sg_profile_enable": [_P, _I32],
     "sg_profile_get": [_P, _I32, ctypes.c_char_p, _SZ, ctypes.POINTER(_I64), ctypes.POINTER(_D)],
+    "sg_sir_run_noalloc": [_P, _P, _P, _I64, _I32, _I64, _I64, _I32, _D, _D, _I32, _I32, _I32, _P],
     "sg_graph_er": [_I64, _D, _U64, _P, _P, ctypes.POINTER(_I64)],
     "sg_graph_ba": [_I64, _I32, _U64, _P, _P, ctypes.POINTER(_I64)],
     "sg_graph_ws": [_I64, _I32, _D, _U64, _P, _P, ctypes.POINTER(_I64)],

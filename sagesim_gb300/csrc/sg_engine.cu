@@ -99,6 +99,9 @@ struct sg_engine {
     }
 };
 
+// Error message for calls without an engine handle (read with sg_last_error(NULL)).
+void sg_set_thread_error(const std::string &msg) { g_create_error = msg; }
+
 #define SG_CK(call)                                                                            \
     do {                                                                                       \
         cudaError_t _ce = (call);                                                              \
