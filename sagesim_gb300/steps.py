@@ -1,0 +1,72 @@
+"""Step objects accepted by Breed.register_step_func.
+
+SAGESim step functions are CuPy-JIT Python kernels (e.g.
+tests/test_simulation.py:24-43). Here a step is one of:
+
+  SIRStep      the hand-written SIR kernels. variant "A" is SAGESim's own SIR
+               step (one Philox draw per agent per tick, salt 1: I recovers if
+               u < p_recovery; S is infected if u < p_infection and any
+               neighbour is infected); variant "B" draws once per infected
+               neighbour (the j-th infected neighbour found draws salt 2 + j).
+  OpinionStep  the float32 opinion update (weighted mean of the first `width`
+               ordered neighbours, Philox N(0, sigma) noise, clamp to [0, 1]).
+  CudaStep     any step written as a CUDA C++ device function against the
+               sg_ctx API of include/sagesim_gb300_step.h, compiled with NVRTC
+               into the tick kernel. Property and global indices are available
+               as PROP_<name> and G_<name> macros.
+
+Globals are referred to by the names given to Model.register_global_property,
+as the reference passes them positionally by registration order
+(sagesim/model.py:2226-2251).
+"""
+import re
+
+
+class SIRStep:
+    def __init__(self, variant="A", state="state", p_infection="p_infection",
+                 p_recovery="p_recovery", codes=(1, 2, 3), strategy=None):
+        if variant not in ("A", "B"):
+            raise ValueError("variant must be 'A' or 'B'")
+        if strategy not in (None, "count", "pull"):
+            raise ValueError("strategy must be None, 'count' or 'pull'")
+        self.variant = variant
+        self.state = state
+        self.p_infection = p_infection
+        self.p_recovery = p_recovery
+        self.codes = tuple(int(c) for c in codes)
+        self.strategy = strategy
+
+    @property
+    def writes(self):
+        return (self.state,)
+
+    def __repr__(self):
+        return "SIRStep(variant=%r, state=%r)" % (self.variant, self.state)
+
+
+class OpinionStep:
+    def __init__(self, opinion="opinion", weights="weights", noise_sigma="noise_sigma"):
+        self.opinion = opinion
+        self.weights = weights
+        self.noise_sigma = noise_sigma
+
+    @property
+    def writes(self):
+        return (self.opinion,)
+
+
+class CudaStep:
+    """A CUDA C++ step: `source` defines `__device__ void <entry>(const sg_ctx&, int i)`."""
+
+    _SET = re.compile(r"set_(?:i32|f32)\s*\(\s*PROP_(\w+)")
+
+    def __init__(self, source, entry, writes=None):
+        self.source = source
+        self.entry = entry
+        if writes is None:
+            writes = sorted(set(self._SET.findall(source)))
+        self._writes = tuple(writes)
+
+    @property
+    def writes(self):
+        return self._writes

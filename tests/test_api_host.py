@@ -1,0 +1,167 @@
+"""Drop-in API bookkeeping on the host (no GPU): Breed, NetworkSpace, CSR
+builder, AgentFactory and Model before setup, and the host arrays setup()
+hands the engine. Mirrors the reference's own unit tests
+(tests/test_breed.py, tests/test_space.py, tests/test_csr.py,
+tests/test_model_lifecycle.py)."""
+from math import nan
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from sagesim_gb300 import Breed, CudaStep, Model, NetworkSpace, SIRStep
+from sagesim_gb300.csr import build_csr_from_ragged, build_csr_values_only
+
+STEP = SIRStep(variant="A")
+
+
+# ---- Breed (tests/test_breed.py) ----
+def test_register_property_scalar_and_list():
+    b = Breed("TestBreed")
+    b.register_property("health", 100)
+    b.register_property("history", [0.0] * 10)
+    assert b.properties["health"] == 100
+    assert b.properties["history"] == [0.0] * 10
+
+
+def test_register_step_func_and_no_double_buffer():
+    b = Breed("TestBreed")
+    b.register_property("counter", 0)
+    b.register_property("result", 0)
+    b.register_step_func(STEP, __file__, priority=0, no_double_buffer=["counter"])
+    fn, path = b.step_funcs[0]
+    assert fn is STEP and path == str(Path(__file__).resolve())
+    assert "counter" in b.no_double_buffer_props and "result" not in b.no_double_buffer_props
+
+
+def test_property_neighbor_visible_and_default_nan():
+    b = Breed("TestBreed")
+    b.register_property("state", 1, neighbor_visible=True)
+    b.register_property("internal", 0, neighbor_visible=False)
+    b.register_property("x")
+    assert b.prop2neighbor_visible["state"] and not b.prop2neighbor_visible["internal"]
+    assert b.properties["x"] != b.properties["x"]  # nan
+
+
+# ---- NetworkSpace (tests/test_space.py) ----
+def make_space(n=3, ordered=False):
+    m = Model(NetworkSpace(ordered=ordered))
+    b = Breed("B")
+    b.register_property("state", 1)
+    m.register_breed(b)
+    for _ in range(n):
+        m.create_agent_of_breed(b)
+    return m, m.get_space()
+
+
+def test_space_connect_disconnect():
+    _, sp = make_space()
+    assert sp._locations == [set(), set(), set()]
+    sp.connect_agents(0, 1)
+    assert 1 in sp._locations[0] and 0 in sp._locations[1]
+    sp.connect_agents(1, 2, directed=True)
+    assert 2 in sp._locations[1] and 1 not in sp._locations[2]
+    sp.disconnect_agents(0, 1)
+    assert 1 not in sp._locations[0] and 0 not in sp._locations[1]
+    sp.connect_agents(0, 2)
+    sp.disconnect_agents(0, 2, directed=True)
+    assert 2 not in sp._locations[0] and 0 in sp._locations[2]
+
+
+def test_ordered_space_keeps_insertion_order_without_duplicates():
+    _, sp = make_space(4, ordered=True)
+    for a, b in [(0, 3), (0, 1), (0, 3), (2, 0)]:
+        sp.connect_agents(a, b)
+    assert sp.get_location(0) == [3, 1, 2]
+
+
+# ---- CSR (tests/test_csr.py golden arrays) ----
+def test_csr_golden():
+    off, val = build_csr_from_ragged([[5, 2], [8, 3, 1], [], [7, 4, 9, 6]])
+    assert off.tolist() == [0, 2, 5, 5, 9] and val.tolist() == [5, 2, 8, 3, 1, 7, 4, 9, 6]
+    off, val = build_csr_from_ragged([{5, 2}, {8}])
+    assert off.tolist() == [0, 2, 3] and set(val[:2].tolist()) == {5, 2} and val[2] == 8
+    off, val = build_csr_from_ragged([])
+    assert off.tolist() == [0] and val.size == 0
+    off, val = build_csr_from_ragged([[1], [], [2, 3]])
+    assert off.tolist() == [0, 1, 1, 3] and val.tolist() == [1, 2, 3]
+    off, _ = build_csr_from_ragged([[10, 20], [30]])
+    assert build_csr_values_only([[100, 200], [300]], off).tolist() == [100, 200, 300]
+
+
+# ---- Model lifecycle (tests/test_model_lifecycle.py, host parts) ----
+def test_model_lifecycle_host():
+    m, _ = make_space(0)
+    b = list(m._agent_factory.breeds)[0]
+    assert [m.create_agent_of_breed(b) for _ in range(5)] == [0, 1, 2, 3, 4]
+    assert m._agent_factory.num_agents == 5
+    m.set_agent_property_value(2, "state", 42)
+    assert m.get_agent_property_value(2, "state") == 42
+    m.register_global_property("rate", 0.5)
+    assert m.get_global_property_value("rate") == 0.5
+    m.set_global_property_value("rate", 0.9)
+    assert m.get_global_property_value("rate") == 0.9
+    m.set_seed(12345)
+    assert m._seed == 12345
+    with pytest.raises(Exception):
+        m.register_breed(Breed("Late"))
+
+
+def test_python_step_function_rejected_with_clear_message():
+    m, _ = make_space(2)
+    b = list(m._agent_factory.breeds)[0]
+    b.register_step_func(lambda *a: None, __file__, priority=0)
+    with pytest.raises(TypeError, match="CudaStep"):
+        m._collect_steps()
+
+
+def test_host_arrays_breed_sort_csr_and_logical_ids():
+    """setup()'s host side: stable breed sort (sagesim/agent.py:438-473), CSR
+    of buffer indices, float32 logical ids (sagesim/model.py:1085-1096)."""
+    m = Model(NetworkSpace())
+    b0, b1 = Breed("A"), Breed("B")
+    for b in (b0, b1):
+        b.register_property("state", 1)
+        b.register_step_func(SIRStep("B"), __file__, 0)
+        m.register_breed(b)
+    m.register_global_property("p_infection", 0.1)
+    m.register_global_property("p_recovery", 0.1)
+    breeds = [0, 1, 0, 1, 1, 0]
+    for i, bi in enumerate(breeds):
+        m.create_agent_of_breed((b0, b1)[bi], state=1 + (i == 3))
+    sp = m.get_space()
+    for a, c in [(0, 1), (1, 2), (3, 4), (5, 0)]:
+        sp.connect_agents(a, c)
+    m.set_agent_logical_id(4, 2**24 + 1)  # rounds to 2^24 in float32
+    m._collect_steps()
+    m._build_host_arrays()
+    assert m._order.tolist() == [0, 2, 5, 1, 3, 4]
+    assert m._breed_ranges == {0: (0, 3), 1: (3, 6)}
+    off, idx = m._csr
+    pos = m._pos
+    for a in range(6):
+        row = set(idx[off[pos[a]]:off[pos[a] + 1]].tolist())
+        assert row == {int(pos[c]) for c in sp._locations[a]}
+    assert m._lids.tolist() == [0, 2, 5, 1, 3, 2**24]
+    dt, w, col = m._props["state"]
+    assert dt == np.int32 and w == 1 and col.tolist() == [1, 1, 1, 1, 2, 1]
+
+
+def test_cuda_step_detects_writes():
+    s = CudaStep("__device__ void f(const sg_ctx& c, int i){ c.set_i32(PROP_counter, i, 10); }", "f")
+    assert s.writes == ("counter",)
+
+
+def test_list_property_padded_with_nan():
+    m = Model(NetworkSpace())
+    b = Breed("B")
+    b.register_property("w", [0.0, 0.0, 0.0])
+    m.register_breed(b)
+    m.create_agent_of_breed(b, w=[1.0, 2.0])
+    m.create_agent_of_breed(b)
+    m._collect_steps()
+    m._build_host_arrays()
+    dt, width, col = m._props["w"]
+    assert width == 3 and dt == np.float32
+    assert col[0, :2].tolist() == [1.0, 2.0] and np.isnan(col[0, 2]) and col[1].tolist() == [0, 0, 0]
+    assert nan != nan

@@ -1,0 +1,334 @@
+"""The drop-in Model API on the GPU against fixtures produced by the reference.
+
+Each case rebuilds, through Breed/Model/NetworkSpace, the model that
+tests/golden/make_golden.py ran through SAGESim's own pipeline, and compares
+the agent states tick by tick: bit-exact for integer state, 1e-6 relative for
+float32 properties.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+from sagesim_gb300 import Breed, CudaStep, Engine, Model, NetworkSpace, OpinionStep, SIRStep, graphs
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def gold(name):
+    return np.load(os.path.join(GOLD, name))
+
+
+class SIRBreed(Breed):
+    def __init__(self, step, name="SIR"):
+        super().__init__(name)
+        self.register_property("state", 1)
+        self.register_step_func(step, __file__, priority=0)
+
+
+def sir_model(step, p_infection, p_recovery, seed, ordered=False):
+    m = Model(NetworkSpace(ordered=ordered))
+    breed = SIRBreed(step)
+    m.register_breed(breed)
+    m.register_global_property("p_infection", p_infection)
+    m.register_global_property("p_recovery", p_recovery)
+    m.set_seed(seed)
+    return m, breed
+
+
+def chain_model(n, p_inf, p_rec, seed, step=None):
+    """tests/test_simulation.py:_build_chain_model with the builtin SIR step."""
+    m, breed = sir_model(step or SIRStep("A"), p_inf, p_rec, seed)
+    for _ in range(n):
+        m.create_agent_of_breed(breed, state=1)
+    m.set_agent_property_value(0, "state", 2)
+    for i in range(n - 1):
+        m.get_space().connect_agents(i, i + 1)
+    return m
+
+
+def states(m, n):
+    return [m.get_agent_property_value(i, "state") for i in range(n)]
+
+
+def test_deterministic_sir_chain_known_answer():
+    """tests/test_simulation.py:95-115."""
+    m = chain_model(10, 1.0, 1.0, 42)
+    m.setup(use_gpu=True)
+    m.simulate(5, sync_workers_every_n_ticks=1)
+    assert states(m, 10) == [3, 3, 3, 3, 3, 2, 1, 1, 1, 1]
+
+
+@pytest.mark.parametrize("key,n,p,seed,ticks", [("det10", 10, (1.0, 1.0), 42, 5),
+                                                 ("sto20_seed999", 20, (0.5, 0.3), 999, 10),
+                                                 ("sto50_seed111", 50, (0.3, 0.2), 111, 20),
+                                                 ("sto50_seed222", 50, (0.3, 0.2), 222, 20)])
+@pytest.mark.parametrize("strategy", ["count", "pull"])
+def test_chain_every_tick_matches_reference(key, n, p, seed, ticks, strategy):
+    hist = gold("chain.npz")[key]
+    m = chain_model(n, p[0], p[1], seed, SIRStep("A", strategy=strategy))
+    m.setup()
+    for t in range(ticks):
+        m.simulate(1)
+        assert m.get_property_array("state").tolist() == hist[t].tolist(), "tick %d" % t
+
+
+def test_seed_reproducibility_and_sensitivity():
+    """tests/test_simulation.py:117-159."""
+    runs = {}
+    for tag, seed in (("a", 999), ("b", 999), ("c", 111), ("d", 222)):
+        m = chain_model(50, 0.3, 0.2, seed)
+        m.setup()
+        m.simulate(20)
+        runs[tag] = states(m, 50)
+    assert runs["a"] == runs["b"]
+    assert runs["c"] != runs["d"]
+
+
+def infect_src():
+    return """
+__device__ void infect(const sg_ctx &c, int i)
+{
+    if (c.i32(PROP_state, i) != 1) return;
+    for (int k = 0; k < c.degree(i); ++k) {
+        if (c.i32(PROP_state, c.neighbor(i, k)) == 2 && c.rand_uniform(i, 1) < c.g[G_p_infection]) {
+            c.set_i32(PROP_state, i, 2);
+            return;
+        }
+    }
+}
+"""
+
+
+def recover_src():
+    return """
+__device__ void recover(const sg_ctx &c, int i)
+{
+    c.set_i32(PROP_dummy, i, c.i32(PROP_dummy, i) + 1);
+    if (c.i32(PROP_state, i) == 2 && c.rand_uniform(i, 2) < c.g[G_p_recovery])
+        c.set_i32(PROP_state, i, 3);
+}
+"""
+
+
+def test_hierarchy_si_and_two_priority_sir():
+    """tests/test_double_buffer.py:247-271 (SI one tick; infection at priority
+    0 and recovery at priority 1, both double-buffered, two ticks)."""
+    d = gold("hier.npz")
+    edges = d["edges"]
+    # SI: builtin SIR-A without recovery
+    m, breed = sir_model(SIRStep("A"), 1.0, 0.0, 0)
+    for _ in range(111):
+        m.create_agent_of_breed(breed, state=1)
+    m.set_agent_property_value(0, "state", 2)
+    for a, b in edges:
+        m.get_space().connect_agents(a, b)
+    m.setup()
+    m.simulate(1)
+    assert m.get_property_array("state").tolist() == d["si_1tick"][0].tolist()
+
+    # SIR with two compiled steps at two priorities and a dummy counter
+    m = Model(NetworkSpace())
+    br = Breed("Infection")
+    br.register_property("state", 1)
+    br.register_property("dummy", 0)
+    br.register_step_func(CudaStep(infect_src(), "infect"), __file__, 0)
+    br.register_step_func(CudaStep(recover_src(), "recover"), __file__, 1)
+    m.register_breed(br)
+    m.register_global_property("p_infection", 1.0)
+    m.register_global_property("p_recovery", 1.0)
+    for _ in range(111):
+        m.create_agent_of_breed(br, state=1)
+    m.set_agent_property_value(0, "state", 2)
+    for a, b in edges:
+        m.get_space().connect_agents(a, b)
+    m.setup()
+    for t in range(2):
+        m.simulate(1)
+        assert m.get_property_array("state").tolist() == d["sir_2ticks"][t].tolist()
+    assert m.get_property_array("dummy").tolist() == [2] * 111
+
+
+def db_model(first, second, nodb):
+    write = CudaStep("__device__ void wc(const sg_ctx &c, int i) { c.set_i32(PROP_counter, i, 10); }", "wc")
+    read = CudaStep("__device__ void rm(const sg_ctx &c, int i) "
+                    "{ c.set_i32(PROP_result, i, c.i32(PROP_counter, i) * 2); }", "rm")
+    steps = {"write": write, "read": read}
+    m = Model(NetworkSpace())
+    br = Breed("DB")
+    br.register_property("counter", 0)
+    br.register_property("result", 0)
+    br.register_step_func(steps[first], __file__, 0, no_double_buffer=["counter"] if nodb else None)
+    br.register_step_func(steps[second], __file__, 1)
+    m.register_breed(br)
+    m.create_agent_of_breed(br, counter=0, result=0)
+    return m
+
+
+@pytest.mark.parametrize("name,first,second,nodb", [("db", "write", "read", False),
+                                                    ("nodb", "write", "read", True),
+                                                    ("rbw_db", "read", "write", False),
+                                                    ("rbw_nodb", "read", "write", True)])
+def test_double_buffer_priority_semantics(name, first, second, nodb):
+    """tests/test_double_buffer.py:282-312 (counter/result by priority order)."""
+    want = json.load(open(os.path.join(GOLD, "db_priority.json")))[name]
+    m = db_model(first, second, nodb)
+    m.setup()
+    m.simulate(1)
+    assert m.get_agent_property_value(0, "counter") == want["counter"]
+    assert m.get_agent_property_value(0, "result") == want["result"]
+
+
+def er_model(step, d, seed=0):
+    off, idx = d["offsets"], d["indices"]
+    n = off.size - 1
+    m, breed = sir_model(step, 0.05, 0.1, seed)
+    m.create_agents_bulk(breed, n, state=d["state0"].astype(np.int32))
+    m.get_space().set_csr(off, idx)
+    return m
+
+
+@pytest.mark.parametrize("variant,key", [("A", "sir_a"), ("B", "sir_b")])
+@pytest.mark.parametrize("strategy", ["count", "pull"])
+def test_er_10k_every_tick_matches_reference(variant, key, strategy):
+    """10,000-agent ER (p=0.001, seed 0), 1 % infected, 100 ticks."""
+    d = gold("er_c1.npz")
+    ref = d[key]
+    m = er_model(SIRStep(variant, strategy=strategy), d)
+    m.setup()
+    for t in range(100):
+        m.simulate(1)
+        got = m.get_property_array("state")
+        assert np.array_equal(got, ref[t]), "tick %d: %d agents differ" % (t, int((got != ref[t]).sum()))
+
+
+def test_er_10k_one_call():
+    d = gold("er_c1.npz")
+    m = er_model(SIRStep("B"), d)
+    m.setup()
+    m.simulate(100)
+    assert np.array_equal(m.get_property_array("state"), d["sir_b"][-1])
+
+
+def test_compiled_sir_step_matches_reference():
+    """The same SIR-A written as a CudaStep (NVRTC path) on the ER fixture."""
+    src = """
+__device__ void sir_a(const sg_ctx &c, int i)
+{
+    const int s = c.i32(PROP_state, i);
+    const double u = c.rand_uniform(i, 1);
+    if (s == 2 && u < c.g[G_p_recovery]) {
+        c.set_i32(PROP_state, i, 3);
+    } else if (s == 1) {
+        for (int k = 0; k < c.degree(i); ++k)
+            if (c.i32(PROP_state, c.neighbor(i, k)) == 2 && u < c.g[G_p_infection])
+                c.set_i32(PROP_state, i, 2);
+    }
+}
+"""
+    d = gold("er_c1.npz")
+    m = er_model(CudaStep(src, "sir_a"), d)
+    m.setup()
+    for t in (0, 9, 49, 99):
+        m.simulate(t + 1 - m.tick)
+        assert np.array_equal(m.get_property_array("state"), d["sir_a"][t]), t
+
+
+def test_two_breeds_and_logical_ids():
+    """Interleaved breeds (sorted into ranges) and explicit logical ids."""
+    d = gold("ba_breeds.npz")
+    off, idx, breeds = d["offsets"], d["indices"], d["breeds"]
+    n = off.size - 1
+    m = Model(NetworkSpace())
+    bl = [SIRBreed(SIRStep("B"), "SIR0"), SIRBreed(SIRStep("B"), "SIR1")]
+    for b in bl:
+        m.register_breed(b)
+    m.register_global_property("p_infection", 0.08)
+    m.register_global_property("p_recovery", 0.1)
+    m.set_seed(77)
+    for i in range(n):
+        m.create_agent_of_breed(bl[int(breeds[i])], state=int(d["state0"][i]))
+    for i in range(n):
+        for k in range(off[i], off[i + 1]):
+            m.get_space().connect_agents(i, int(idx[k]), directed=True)
+    for a, l in d["lid_pairs"]:
+        m.set_agent_logical_id(int(a), int(l))
+    m.setup()
+    for t in range(30):
+        m.simulate(1)
+        assert np.array_equal(m.get_property_array("state"), d["history"][t]), t
+    assert m.get_breed_data("SIR1", "state") == \
+        d["history"][-1][np.flatnonzero(breeds == 1)].tolist()
+
+
+def test_opinion_model_matches_reference():
+    """float32 opinion + float32[8] weights on ordered neighbours (WS 2,000)."""
+    d = gold("opinion_ws.npz")
+    off, idx = d["offsets"], d["indices"]
+    n = off.size - 1
+    m = Model(NetworkSpace(ordered=True))
+    br = Breed("Opinion")
+    br.register_property("opinion", 0.0)
+    br.register_property("weights", [0.0] * 8)
+    br.register_step_func(OpinionStep(), __file__, 0)
+    m.register_breed(br)
+    m.register_global_property("noise_sigma", 0.01)
+    m.set_seed(2)
+    m.create_agents_bulk(br, n, opinion=d["opinion0"], weights=d["weights"])
+    m.get_space().set_csr(off, idx)
+    m.setup()
+    for t, want in zip(d["ticks"], d["history"]):
+        m.simulate(int(t) - m.tick)
+        got = m.get_property_array("opinion")
+        rel = np.abs(got - want) / np.maximum(np.abs(want), 1e-30)
+        ok = (rel <= 1e-6) | (np.abs(got - want) <= 1e-12)
+        assert ok.all(), "tick %d: max rel %g" % (t, rel[~ok].max())
+
+
+def test_opinion_engine_vs_oracle_larger():
+    """WS 200,000 agents, 100 ticks, engine builtin vs the CPU oracle."""
+    off, idx = graphs.watts_strogatz(200_000, 10, 0.1, 2)
+    n = off.size - 1
+    rng = np.random.default_rng(2)
+    x0 = rng.random(n, dtype=np.float32)
+    w = rng.standard_normal((n, 8), dtype=np.float32)
+    with Engine() as e:
+        e.set_graph(off, idx, ordered=True)
+        e.set_seed(2)
+        px = e.add_property("opinion", np.float32, init=x0)
+        pw = e.add_property("weights", np.float32, width=8, init=w)
+        e.add_opinion(px, pw, 0.01)
+        e.run(0, 100, stats=False)
+        got = e.get_property(px)
+    want, _ = oracle.opinion_run(off, idx, w, x0, 2, 0, 100, 0.01)
+    rel = np.abs(got - want) / np.maximum(np.abs(want), 1e-30)
+    ok = (rel <= 1e-6) | (np.abs(got - want) <= 1e-12)
+    assert ok.all(), "max rel %g over %d agents" % (rel[~ok].max(), int((~ok).sum()))
+
+
+def test_set_property_between_simulates_and_reset():
+    m = chain_model(10, 1.0, 1.0, 42)
+    m.setup()
+    m.simulate(2)
+    m.set_agent_property_value(9, "state", 2)  # a second outbreak at the far end
+    m.simulate(1)
+    s = states(m, 10)
+    assert s[9] == 3 and s[8] == 2 and s[2] == 3 and s[3] == 2
+    m.reset()
+    assert m.tick == 0
+    assert m.get_agent_property_value(3, "state") == 2  # host store refreshed from the device
+    m.simulate(1)
+    assert states(m, 10)[4] == 2
+
+
+def test_global_change_between_simulates():
+    m = chain_model(10, 0.0, 0.0, 42)
+    m.setup()
+    m.simulate(3)
+    assert states(m, 10) == [2] + [1] * 9
+    m.set_global_property_value("p_infection", 1.0)
+    m.simulate(1)
+    assert states(m, 10)[:3] == [2, 2, 1]
