@@ -184,6 +184,109 @@ int sg_profile_enable(sg_engine *e, int32_t on);
 int sg_profile_get(sg_engine *e, int32_t kind, char *name, size_t cap, int64_t *launches,
                    double *total_ms);
 
+/* ---- ensembles: many independent SIR scenarios in one launch per tick ---------------
+ * No single counterpart in the reference, which runs one model per process
+ * (sagesim/model.py:961-998); each scenario here is what one reference Model
+ * with one SIR breed would simulate, and stays bit-exact with its standalone
+ * run: it keeps its own seed, logical ids, tick counter (starting at 0) and
+ * horizon. Scenarios are packed into one device pool (global CSR, state,
+ * segment table, tile list); every kernel launch advances all of them. The
+ * tick loop of sg_batch_run is captured once as a CUDA graph and replayed. */
+typedef struct sg_batch sg_batch;
+
+typedef struct sg_scenario_desc {
+    int64_t n_agents;          /* agents of the scenario                                   */
+    int64_t nnz;               /* CSR entries                                              */
+    const int32_t *offsets;    /* host CSR (local indices), copied                         */
+    const int32_t *indices;
+    const int32_t *state;      /* host initial state, n_agents int32                      */
+    const int64_t *lids;       /* host RNG keys or NULL (= local agent index)              */
+    int64_t seed;
+    double beta, gamma;
+    int32_t builtin;           /* SG_BUILTIN_SIR_A or SG_BUILTIN_SIR_B (same for a batch)  */
+    int32_t code_s, code_i, code_r;
+    int32_t horizon;           /* ticks the scenario runs; later ticks skip it             */
+    int32_t flags;             /* SG_GRAPH_SYMMETRIC when the CSR is its own transpose     */
+} sg_scenario_desc;
+
+/* Launch configuration the autotuner chooses between (all give identical results). */
+typedef struct sg_tune {
+    int32_t strategy;          /* SG_SIR_PULL or SG_SIR_COUNT                     */
+    int32_t blocks_per_sm;     /* persistent grid = blocks_per_sm x SM count     */
+    int32_t thread_row;        /* rows up to this length: one lane; longer: warp */
+    int32_t mega_row;          /* rows longer than this: a whole block           */
+    double us_per_tick;        /* measured by sg_batch_tune (output)             */
+} sg_tune;
+
+int sg_batch_create(const sg_engine_cfg *cfg, sg_batch **out);
+int sg_batch_destroy(sg_batch *b);
+int sg_batch_last_error(const sg_batch *b, char *buf, size_t cap);
+/* Stages a scenario (host copy); returns its id. Validates the CSR. */
+int sg_batch_add_scenario(sg_batch *b, const sg_scenario_desc *d, int32_t *sid);
+/* Packs the staged scenarios into the device pool (once, before running). */
+int sg_batch_commit(sg_batch *b);
+int sg_batch_set_tune(sg_batch *b, const sg_tune *t);
+int sg_batch_get_tune(sg_batch *b, sg_tune *t);
+/* Times every candidate launch configuration on `ticks` ticks from the
+ * current state (restored afterwards), keeps the fastest and returns it. */
+int sg_batch_tune(sg_batch *b, int32_t ticks, sg_tune *best);
+/* Advances every scenario by up to nticks ticks (none past its horizon).
+ * use_graph: replay a captured CUDA graph of the tick loop. Asynchronous. */
+int sg_batch_run(sg_batch *b, int32_t nticks, int32_t use_graph);
+int sg_batch_synchronize(sg_batch *b);
+/* Current state of a scenario (host copy, synchronous) and its tick count. */
+int sg_batch_get_state(sg_batch *b, int32_t sid, int32_t *host, int64_t n);
+int sg_batch_scenario_tick(sg_batch *b, int32_t sid, int64_t *tick);
+/* Totals of the batch: agents, CSR entries, device bytes held. */
+int sg_batch_info(sg_batch *b, int64_t *agents, int64_t *nnz, int64_t *device_bytes);
+/* Device snapshot of the state of every scenario (and its tick) and restore. */
+int sg_batch_snapshot(sg_batch *b);
+int sg_batch_restore(sg_batch *b);
+
+/* ---- serving: continuous batching of scenario requests ----------------------------------
+ * No counterpart in the reference. Requests (one SIR scenario each, with its
+ * own horizon) are admitted FIFO against an HBM budget and the free space of a
+ * resident scenario pool; every sg_server_step admits what fits, advances all
+ * resident scenarios together by nticks (one CUDA-graph replay), and retires
+ * the ones that reached their horizon, whose final state is kept on the host
+ * until taken. A request never sees another's data: each result equals the
+ * scenario's standalone run. A request larger than the whole budget or pool is
+ * refused at submission with SG_ERR_BUDGET. A request passed over 8 times by
+ * smaller ones that fitted stops later requests from being admitted ahead of it. */
+typedef struct sg_server sg_server;
+
+typedef struct sg_server_cfg {
+    int32_t device;
+    int32_t builtin;         /* SIR variant of every request                       */
+    void *stream;            /* NULL = server-owned stream                         */
+    int64_t budget_bytes;    /* admission budget for resident scenarios            */
+    int64_t agent_slots;     /* device pool capacity: agents (+1 per scenario)      */
+    int64_t edge_slots;      /* device pool capacity: CSR entries                   */
+    int32_t max_resident;    /* scenarios resident at once                          */
+    int32_t flags;           /* reserved, 0                                         */
+} sg_server_cfg;
+
+#define SG_REQ_QUEUED 0
+#define SG_REQ_RUNNING 1
+#define SG_REQ_DONE 2
+
+int sg_server_create(const sg_server_cfg *cfg, sg_server **out);
+int sg_server_destroy(sg_server *s);
+int sg_server_last_error(const sg_server *s, char *buf, size_t cap);
+/* Queues a request (host arrays are copied); the CSR must be symmetric. */
+int sg_server_submit(sg_server *s, const sg_scenario_desc *d, int64_t *rid);
+/* Admits, runs nticks for every resident scenario, retires the finished ones.
+ * Synchronous. n_done (nullable) = requests finished by this step. */
+int sg_server_step(sg_server *s, int32_t nticks, int32_t *n_done);
+/* status = SG_REQ_*; tick = ticks done so far. */
+int sg_server_poll(sg_server *s, int64_t rid, int32_t *status, int64_t *tick);
+/* Copies a finished request's final state and forgets the request. */
+int sg_server_take_result(sg_server *s, int64_t rid, int32_t *host, int64_t n);
+int sg_server_counts(sg_server *s, int64_t *queued, int64_t *resident, int64_t *done,
+                     int64_t *resident_bytes);
+/* Sets the launch configuration of the resident pool (see sg_tune). */
+int sg_server_set_tune(sg_server *s, const sg_tune *t);
+
 /* ---- allocation-free SIR ticks ------------------------------------------------------
  * No counterpart in the reference. For callers that cannot allocate device
  * memory (their memory is owned by a pool or plan of their own, they run while

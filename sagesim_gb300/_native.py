@@ -34,6 +34,10 @@ SG_BUILTIN_OPINION = 3
 SG_SIR_PULL = 0
 SG_SIR_COUNT = 1
 
+SG_REQ_QUEUED = 0
+SG_REQ_RUNNING = 1
+SG_REQ_DONE = 2
+
 SG_GRAPH_ORDERED = 1
 SG_GRAPH_SYMMETRIC = 2
 
@@ -72,8 +76,21 @@ class ScenarioDesc(ctypes.Structure):
                 ("offsets", ctypes.c_void_p), ("indices", ctypes.c_void_p),
                 ("state", ctypes.c_void_p), ("lids", ctypes.c_void_p),
                 ("seed", ctypes.c_int64), ("beta", ctypes.c_double), ("gamma", ctypes.c_double),
-                ("variant", ctypes.c_int32), ("code_s", ctypes.c_int32), ("code_i", ctypes.c_int32),
+                ("builtin", ctypes.c_int32), ("code_s", ctypes.c_int32), ("code_i", ctypes.c_int32),
                 ("code_r", ctypes.c_int32), ("horizon", ctypes.c_int32), ("flags", ctypes.c_int32)]
+
+
+class Tune(ctypes.Structure):
+    _fields_ = [("strategy", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
+                ("thread_row", ctypes.c_int32), ("mega_row", ctypes.c_int32),
+                ("us_per_tick", ctypes.c_double)]
+
+
+class ServerCfg(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("builtin", ctypes.c_int32), ("stream", ctypes.c_void_p),
+                ("budget_bytes", ctypes.c_int64), ("agent_slots", ctypes.c_int64),
+                ("edge_slots", ctypes.c_int64), ("max_resident", ctypes.c_int32),
+                ("flags", ctypes.c_int32)]
 
 
 _P = ctypes.c_void_p
@@ -107,6 +124,31 @@ SIGNATURES = {
     "sg_restore": [_P],
     "sg_profile_enable": [_P, _I32],
     "sg_profile_get": [_P, _I32, ctypes.c_char_p, _SZ, ctypes.POINTER(_I64), ctypes.POINTER(_D)],
+    "sg_batch_create": [ctypes.POINTER(EngineCfg), ctypes.POINTER(_P)],
+    "sg_batch_destroy": [_P],
+    "sg_batch_last_error": [_P, ctypes.c_char_p, _SZ],
+    "sg_batch_add_scenario": [_P, ctypes.POINTER(ScenarioDesc), ctypes.POINTER(_I32)],
+    "sg_batch_commit": [_P],
+    "sg_batch_set_tune": [_P, ctypes.POINTER(Tune)],
+    "sg_batch_get_tune": [_P, ctypes.POINTER(Tune)],
+    "sg_batch_tune": [_P, _I32, ctypes.POINTER(Tune)],
+    "sg_batch_run": [_P, _I32, _I32],
+    "sg_batch_synchronize": [_P],
+    "sg_batch_get_state": [_P, _I32, _P, _I64],
+    "sg_batch_scenario_tick": [_P, _I32, ctypes.POINTER(_I64)],
+    "sg_batch_info": [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I64)],
+    "sg_batch_snapshot": [_P],
+    "sg_batch_restore": [_P],
+    "sg_server_create": [ctypes.POINTER(ServerCfg), ctypes.POINTER(_P)],
+    "sg_server_destroy": [_P],
+    "sg_server_last_error": [_P, ctypes.c_char_p, _SZ],
+    "sg_server_submit": [_P, ctypes.POINTER(ScenarioDesc), ctypes.POINTER(_I64)],
+    "sg_server_step": [_P, _I32, ctypes.POINTER(_I32)],
+    "sg_server_poll": [_P, _I64, ctypes.POINTER(_I32), ctypes.POINTER(_I64)],
+    "sg_server_take_result": [_P, _I64, _P, _I64],
+    "sg_server_counts": [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I64),
+                         ctypes.POINTER(_I64)],
+    "sg_server_set_tune": [_P, ctypes.POINTER(Tune)],
     "sg_sir_run_noalloc": [_P, _P, _P, _I64, _I32, _I64, _I64, _I32, _D, _D, _I32, _I32, _I32, _P],
     "sg_graph_er": [_I64, _D, _U64, _P, _P, ctypes.POINTER(_I64)],
     "sg_graph_ba": [_I64, _I32, _U64, _P, _P, ctypes.POINTER(_I64)],
@@ -139,13 +181,13 @@ def load(build_if_missing=True):
         return lib
 
 
-def last_error(handle):
+def last_error(handle, fn="sg_last_error"):
     buf = ctypes.create_string_buffer(4096)
-    load().sg_last_error(handle, buf, len(buf))
+    getattr(load(), fn)(handle, buf, len(buf))
     return buf.value.decode(errors="replace")
 
 
-def check(rc, handle=None):
+def check(rc, handle=None, fn="sg_last_error"):
     if rc != SG_OK:
-        raise SageSimError(rc, last_error(handle))
+        raise SageSimError(rc, last_error(handle, fn))
     return rc

@@ -1,0 +1,127 @@
+// sg_batch.h -- the scenario pool shared by the ensemble batch and the server.
+//
+// A pool holds many independent SIR scenarios in one set of device arrays:
+//   agent slots  [agent_base, agent_base + n + 1): the extra slot keeps each
+//                scenario's offsets self-contained (off[agent_base + n] is the
+//                end of its last row), so scenarios can come and go;
+//   edge slots   [edge_base, edge_base + nnz): CSR entries as global indices;
+//   state        int32 per agent slot (updated in place by the count strategy;
+//                the pull strategy ping-pongs with a second buffer);
+//   cnt/changes  count-strategy scratch per agent slot;
+//   segs         one SgSeg per scenario (tick counter, horizon, seed, codes);
+//   tiles        the work list of the kernels, tiles never straddle scenarios.
+// Space is handed out first-fit from free lists of agent and edge slots.
+#pragma once
+#include <map>
+#include <string>
+#include <vector>
+
+#include "sg_internal.h"
+
+struct SgPoolScen {
+    int32_t sid = -1;
+    int64_t n = 0, nnz = 0;
+    int64_t agent_base = -1, edge_base = -1;
+    int64_t tick = 0;     // ticks done
+    int64_t horizon = 0;  // ticks to do
+    int32_t par = 0;      // state lives in buffer [par] (pull ping-pong)
+    bool cnt_valid = false;
+    sg_scenario_desc d{}; // host pointers are not kept
+    uint32_t key = 0, kinf = 0, krec = 0;
+    std::vector<uint32_t> lids; // empty: lid = local index
+    bool symmetric = true;
+};
+
+// Free-list allocator over [0, cap) (first fit, coalescing on release).
+struct SgRanges {
+    int64_t cap = 0;
+    std::map<int64_t, int64_t> free_; // start -> length
+    void reset(int64_t c)
+    {
+        cap = c;
+        free_.clear();
+        if (c > 0) free_[0] = c;
+    }
+    int64_t take(int64_t len);
+    void give(int64_t start, int64_t len);
+    int64_t largest() const;
+};
+
+struct SgPool {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int sm_count = 152;
+    std::string err;
+
+    int64_t agent_cap = 0, edge_cap = 0;
+    SgRanges agents, edges;
+    SgDev off, idx, toff, tidx, st[2], cnt, changes, tile_nch, lids, segs, tiles, mega;
+    SgDev snap_st[2], snap_cnt;
+    bool any_lids = false, all_symmetric = true;
+    int64_t seg_cap = 0, tile_cap = 0, mega_cap = 0;
+
+    std::vector<SgPoolScen> scen; // by slot; sid -> slot via sid_slot
+    std::map<int32_t, size_t> sid_slot;
+    int32_t next_sid = 0;
+    int32_t builtin = 0; // SIR variant shared by the pool
+
+    std::vector<SgSeg> hsegs;
+    std::vector<SgTile> htiles;
+    std::vector<SgMega> hmega;
+    bool tables_dirty = true;
+    uint64_t version = 1;
+
+    sg_tune tune{SG_SIR_COUNT, 8, 32, 2048, 0.0};
+    cudaGraphExec_t graph = nullptr;
+    int32_t graph_nticks = -1;
+    uint64_t graph_version = 0;
+    sg_tune graph_tune{};
+
+    int fail(int code, const std::string &m)
+    {
+        err = m;
+        return code;
+    }
+    int cuda_fail(cudaError_t ce, const char *what)
+    {
+        err = std::string(what) + ": " + cudaGetErrorString(ce);
+        return ce == cudaErrorMemoryAllocation ? SG_ERR_OOM : SG_ERR_CUDA;
+    }
+
+    int init(const sg_engine_cfg *cfg);
+    void destroy();
+    // Device arrays for the given capacities (contents of a smaller pool are
+    // not kept: call before placing scenarios).
+    int allocate(int64_t agent_cap, int64_t edge_cap, int64_t max_scen, bool transpose, bool lids);
+    // Validates and places one scenario (uploads CSR, state, lids).
+    int place(const sg_scenario_desc &d, const int32_t *off, const int32_t *idx, const int32_t *state,
+              const int64_t *lids, int32_t sid);
+    void release(int32_t sid);
+    bool fits(int64_t n, int64_t nnz) const;
+    int rebuild_tables();
+    // Enqueues nticks ticks (and the count-strategy init where needed).
+    int run(int32_t nticks, bool use_graph);
+    int snapshot();
+    int restore();
+    int get_state(int32_t sid, int32_t *host, int64_t n);
+    int consolidate(); // moves every scenario's state to buffer 0
+    size_t device_bytes() const;
+
+    // scenario id -> its rows longer than the smallest tunable mega_row
+    // (local agent, length)
+    std::map<int32_t, std::vector<std::pair<int32_t, int32_t>>> s_long_rows_;
+    struct SnapHost {
+        int64_t tick;
+        int32_t par;
+        bool cnt_valid;
+    };
+    std::vector<SnapHost> snap_host_;
+
+  private:
+    int enqueue(int32_t nticks, bool capturing);
+    int upload_segs();
+};
+
+// bytes of device memory a scenario of n agents and nnz entries occupies
+int64_t sg_pool_scenario_bytes(int64_t n, int64_t nnz, bool transpose, bool lids);

@@ -555,7 +555,7 @@ static SgTickArgs base_args(sg_engine *e, SgStep *s, int32_t r, bool inplace)
     a.tiles = s->tiles.as<SgTile>();
     a.ntiles = s->ntiles;
     a.r = r;
-    a.hub_deg = e->hub_deg;
+    a.thread_row = e->hub_deg;
     a.mega = s->mega.as<SgMega>();
     a.nmega = s->nmega;
     a.mega_blocks = std::min(s->nmega, e->sm_count);

@@ -78,7 +78,12 @@ __device__ __forceinline__ uint32_t seg_lid(const SgSeg &sg, int32_t i)
 // than that ("mega" rows, a few dozen in a 10^7-agent power-law graph) are
 // listed at setup and scanned by dedicated blocks (1024 entries per step).
 constexpr int kBatch = 4;
-constexpr int32_t kThreadRow = 32;
+constexpr int32_t kThreadRow = 32; // default of SgTickArgs::thread_row
+
+__device__ __forceinline__ int32_t thread_row_of(const SgTickArgs &a)
+{
+    return a.thread_row > 0 ? a.thread_row : kThreadRow;
+}
 
 // Number of infected entries among row[k .. min(k+4, e)), e > k.
 __device__ __forceinline__ int batch_count(const int32_t *__restrict__ idx,
@@ -277,6 +282,7 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_pull_kernel(SgTickArgs a)
         const uint32_t key = sg.key, kinf = sg.kinf, krec = sg.krec;
         const int32_t cs = sg.cs, ci = sg.ci, cr = sg.cr;
         const int32_t mega_row = a.mega_row;
+        const int32_t thread_row = thread_row_of(a);
         unsigned long long nS = 0, nI = 0, nR = 0, eS = 0;
 
         for (int32_t wbase = tile.begin + warp * 32; wbase < tile.end; wbase += SG_SIR_THREADS) {
@@ -300,7 +306,7 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_pull_kernel(SgTickArgs a)
                     } else {
                         if (STATS) eS += (unsigned long long)(e - b);
                         if (lucky) {
-                            if (e - b > kThreadRow)
+                            if (e - b > thread_row)
                                 medium = true;
                             else if (VARIANT == 1 ? any_infected_thread(idx, sin, b, e, ci)
                                                   : trials_thread(idx, sin, b, e, ci, c0b, lid, key,
@@ -375,7 +381,7 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_init_kernel(SgTickAr
                 e = a.off[i + 1];
                 if (e - b > a.mega_row) {
                     // mega block
-                } else if (e - b > kThreadRow) {
+                } else if (e - b > thread_row_of(a)) {
                     medium = true;
                 } else {
                     a.cnt[i] = count_thread(a.idx, sin, b, e, ci);
@@ -514,7 +520,7 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_scatter_kernel(SgTic
                 b = __ldg(a.toff + g);
                 e = __ldg(a.toff + g + 1);
             }
-            const bool long_row = e - b > kThreadRow;
+            const bool long_row = e - b > thread_row_of(a);
             if (!long_row) {
                 for (int32_t k = b; k < e; k += 4) {
                     const int32_t last = e - 1;

@@ -47,7 +47,8 @@ struct SgTickArgs {
     const SgTile *tiles;
     int32_t ntiles;
     int32_t r;              // tick relative to the run start
-    int32_t hub_deg;        // unused (rows <= 32 are lane-scanned, longer warp-scanned)
+    int32_t thread_row;     // rows up to this length are scanned by one lane, longer
+                            // ones by a warp (0 = default 32)
     const SgMega *mega;     // rows longer than mega_row, scanned by whole blocks
     int32_t nmega;
     int32_t mega_blocks;    // the last mega_blocks blocks of the grid take mega rows
