@@ -125,6 +125,44 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def algorithmic_bytes(kernel, n, st0, tick_stats, active):
+    """Compulsory DRAM bytes per launch of `kernel`, per tick of the run (int32 state).
+
+    sir_pull          12 B per agent (state read/write, row offset) + 4 B per CSR
+                      entry of the tick-start susceptible agents (E_S)
+    sir_count_step    4 B state read per agent, 4 B count read per tick-start S
+                      agent, 8 B per transition (state write + change entry)
+    frontier_step     20 B per active agent (list, state, count, mark, next list)
+                      + 8 B per transition
+    *_scatter         8 B per transition (change entry, transpose offsets) + 12 B
+                      per transpose entry of a changed agent (index read, count
+                      read-modify-write); recoveries' degree sum is estimated from
+                      the infections' mean degree
+    """
+    S = tick_stats[:, 0].astype(np.float64)
+    R = tick_stats[:, 2].astype(np.float64)
+    S_start = np.concatenate([[float((st0 == CODES[0]).sum())], S[:-1]])
+    R_start = np.concatenate([[float((st0 == CODES[2]).sum())], R[:-1]])
+    inf = S_start - S
+    rec = R - R_start
+    changes = inf + rec
+    E_S = tick_stats[:, 3].astype(np.float64)
+    deg_inf = E_S - np.concatenate([E_S[1:], [E_S[-1]]])
+    mean_deg = deg_inf.sum() / max(inf.sum(), 1.0)
+    deg_changes = deg_inf + rec * mean_deg
+    if kernel == "sir_pull":
+        return 12.0 * n + 4.0 + 4.0 * E_S
+    if kernel == "sir_count_step":
+        return 4.0 * n + 4.0 * S_start + 8.0 * changes
+    if kernel == "frontier_step":
+        return 20.0 * active + 8.0 * changes
+    if kernel in ("sir_count_scatter", "frontier_scatter"):
+        return 8.0 * changes + 12.0 * deg_changes
+    # sir_count_init, once per run: state of every agent, offsets, CSR rows and
+    # count write of the susceptible agents
+    return np.array([4.0 * n + 12.0 * S_start[0] + 4.0 * E_S[0]])
+
+
 def cpu_port_rate(off, idx, st, lids, ticks, threads=0):
     """Agent-ticks/s of the C port of the tick (oracle/) on the host cores."""
     from oracle import oracle
@@ -178,10 +216,13 @@ def profile_case(args):
         eng.set_seed(SEED)
         prop = eng.add_property("state", np.int32, init=st0)
         eng.add_sir(prop, BETA, GAMMA, variant="B", strategy=args.strategy, codes=CODES)
-        eng.run(0, TICKS, stats=False)
+        stats, _ = eng.run(0, TICKS, stats=True)
+        active = eng.last_run_active(TICKS)
         final = eng.get_property(prop)
     print("profile case done: %d agents, %d ticks, %d infected or recovered at the end"
           % (args.agents, TICKS, int((final != CODES[0]).sum())))
+    for t in (0, 5, 10, 15, 20, 25, 30, 40, 60, 100, 150, 199):
+        print("tick %3d  S %9d  I %9d  R %9d  E_S %10d  processed %9d" % ((t,) + tuple(stats[t]) + (active[t],)))
 
 
 def main():
@@ -190,7 +231,7 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--strategy", default="count", choices=["count", "pull"])
+    ap.add_argument("--strategy", default="count", choices=["count", "frontier", "pull"])
     ap.add_argument("--agents", type=int, default=N_AGENTS)
     ap.add_argument("--profile-case", action="store_true",
                     help="run one simulate(200) of --strategy and exit (for ncu captures)")
@@ -234,6 +275,7 @@ def main():
             eng.snapshot()
             # trajectory statistics (untimed): E_S per tick for edge-visits/s and bytes
             tick_stats, _ = eng.run(0, TICKS, stats=True)
+            active = eng.last_run_active(TICKS).astype(np.float64)
             final = eng.get_property(prop)
             eng.restore()
 
@@ -288,28 +330,17 @@ def main():
             eng.profile(False)
             eng.close()
         dom_name, (dom_launches, dom_ms) = max(rep.items(), key=lambda kv: kv[1][1])
-        S = tick_stats[:, 0].astype(np.float64)
-        S_start = np.concatenate([[float((st0 == CODES[0]).sum())], S[:-1]])
-        R = tick_stats[:, 2].astype(np.float64)
-        R_start = np.concatenate([[float((st0 == CODES[2]).sum())], R[:-1]])
-        changes = (S_start - S) + (R - R_start)  # S->I and I->R transitions
+        alg = algorithmic_bytes(dom_name, n, st0, tick_stats, active)
         E_S = tick_stats[:, 3].astype(np.float64)
-        if dom_name == "sir_count_step":
-            # state read for every agent, count read for tick-start S agents,
-            # state write + change-list entry per transition
-            alg = 4.0 * n + 4.0 * S_start + 8.0 * changes
-        elif dom_name == "sir_count_scatter":
-            alg = 4.0 * changes
-        else:  # pull: 12 B per agent + 4 B per CSR entry of tick-start S agents
-            alg = 12.0 * n + 4.0 + 4.0 * E_S
         alg_per_launch = float(alg.mean())
         per_launch_ms = dom_ms / max(dom_launches, 1)
         achieved = alg_per_launch / (per_launch_ms / 1e3) / 1e9
-        kernels_per_tick = 2 if strategy == "count" else 1
+        kernels_per_tick = 1 if strategy == "pull" else 2
+        setup_launches = {"pull": 0, "count": 1, "frontier": 2}[strategy]
         return {
             "value": world * n * TICKS / (ms_step / 1e3), "ms_per_step": ms_step,
             "e2e": world * n * TICKS / e2e_s, "edge_visits_per_s": world * float(E_S.sum()) / (ms_step / 1e3),
-            "launches": steps * (TICKS * kernels_per_tick + (1 if strategy == "count" else 0)),
+            "launches": steps * (TICKS * kernels_per_tick + setup_launches),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "kernel": dom_name,
                          "peak_source": peak_kind, "per_launch_us": per_launch_ms * 1e3,
@@ -319,7 +350,7 @@ def main():
         }
 
     results = {}
-    for strategy in [args.strategy] + [s for s in ("count", "pull") if s != args.strategy]:
+    for strategy in [args.strategy] + [s for s in ("count", "frontier", "pull") if s != args.strategy]:
         results[strategy] = measure(strategy, args.steps, args.warmup)
     head = results[args.strategy]
     for s_, r_ in results.items():

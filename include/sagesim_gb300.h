@@ -77,6 +77,10 @@ extern "C" {
  * updates it only for agents whose state changed (needs the transpose CSR,
  * built once per graph). */
 #define SG_SIR_COUNT 1
+/* Frontier: like count, but each tick touches only the active agents
+ * (infected, or susceptible with an infected neighbour), kept in a compact
+ * list; the SIR step must be the engine's only step (state updated in place). */
+#define SG_SIR_FRONTIER 2
 
 /* ---- graph flags ------------------------------------------------------------ */
 /* Row order matters (NetworkSpace(ordered=True), sagesim/space.py:54-71). */
@@ -172,6 +176,11 @@ int sg_run(sg_engine *e, int64_t tick0, int32_t nticks, int64_t *tick_stats, sg_
  * CUDA graph of the tick loop when use_graph != 0). No stats. */
 int sg_run_async(sg_engine *e, int64_t tick0, int32_t nticks, int32_t use_graph);
 int sg_synchronize(sg_engine *e);
+
+/* Agents the SIR step processed in each tick of the last sg_run/sg_run_async
+ * (the active list length for the frontier strategy, the step's agent range
+ * otherwise); n = number of ticks to report. Synchronizes the stream. */
+int sg_last_run_active(sg_engine *e, int64_t *out, int32_t n);
 
 /* Device snapshot of every property (checkpoint in HBM) and restore. */
 int sg_snapshot(sg_engine *e);

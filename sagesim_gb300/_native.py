@@ -33,6 +33,7 @@ SG_BUILTIN_OPINION = 3
 
 SG_SIR_PULL = 0
 SG_SIR_COUNT = 1
+SG_SIR_FRONTIER = 2
 
 SG_REQ_QUEUED = 0
 SG_REQ_RUNNING = 1
@@ -120,6 +121,7 @@ SIGNATURES = {
     "sg_run": [_P, _I64, _I32, _P, ctypes.POINTER(Stats)],
     "sg_run_async": [_P, _I64, _I32, _I32],
     "sg_synchronize": [_P],
+    "sg_last_run_active": [_P, _P, _I32],
     "sg_snapshot": [_P],
     "sg_restore": [_P],
     "sg_profile_enable": [_P, _I32],

@@ -75,11 +75,13 @@ struct sg_engine {
 
     // scratch of the count strategy and of per-tick statistics
     SgDev cnt, changes, tile_nch, stats;
+    SgDev flist[2], flen, fnch, fmark, fstats_init, fstats_delta; // frontier strategy
     SgDev transpose_tmp, scan_tmp;
     SgDev prop_table; // sg_prop_dev per property, for compiled steps
 
     SgProfiler prof;
     int hub_deg = 32;
+    int32_t last_nticks = 0;
 
     // CUDA graph of the tick loop (sg_run_async with use_graph)
     cudaGraphExec_t graph_exec = nullptr;
@@ -362,7 +364,7 @@ int sg_add_builtin_step(sg_engine *e, const sg_builtin_params *bp, int32_t *step
         return e->fail(SG_ERR_INVALID, "step agent range out of bounds");
     if (bp->builtin == SG_BUILTIN_SIR_A || bp->builtin == SG_BUILTIN_SIR_B) {
         if (sp.dtype != SG_I32) return e->fail(SG_ERR_INVALID, "SIR state must be int32");
-        if (bp->strategy != SG_SIR_PULL && bp->strategy != SG_SIR_COUNT)
+        if (bp->strategy != SG_SIR_PULL && bp->strategy != SG_SIR_COUNT && bp->strategy != SG_SIR_FRONTIER)
             return e->fail(SG_ERR_INVALID, "unknown SIR strategy");
     } else if (bp->builtin == SG_BUILTIN_OPINION) {
         if (sp.dtype != SG_F32) return e->fail(SG_ERR_INVALID, "opinion must be float32");
@@ -374,8 +376,8 @@ int sg_add_builtin_step(sg_engine *e, const sg_builtin_params *bp, int32_t *step
     for (auto &s : e->steps)
         if (s->kind == SG_BUILTIN_SIR_A || s->kind == SG_BUILTIN_SIR_B)
             if ((bp->builtin == SG_BUILTIN_SIR_A || bp->builtin == SG_BUILTIN_SIR_B) &&
-                s->bp.strategy == SG_SIR_COUNT && bp->strategy == SG_SIR_COUNT)
-                return e->fail(SG_ERR_INVALID, "one count-strategy SIR step per engine");
+                s->bp.strategy != SG_SIR_PULL && bp->strategy != SG_SIR_PULL)
+                return e->fail(SG_ERR_INVALID, "one count- or frontier-strategy SIR step per engine");
     auto s = std::make_unique<SgStep>();
     s->id = e->next_step_id++;
     s->kind = bp->builtin;
@@ -442,8 +444,9 @@ struct SgPlan {
     std::vector<SgStep *> order;             // by (priority, insertion)
     std::vector<int32_t> copy_props;         // double-buffered props needing copy-through
     std::vector<int32_t> swap_props;         // double-buffered props written this tick
-    SgStep *count_step = nullptr;
-    bool count_inplace = false; // the count step is the only step: state updated in place
+    SgStep *count_step = nullptr; // the SIR step keeping infected-neighbour counts
+    bool count_inplace = false;   // it is the only step: state updated in place
+    bool frontier = false;        // it uses the frontier strategy
 };
 
 static SgPlan make_plan(sg_engine *e)
@@ -463,10 +466,11 @@ static SgPlan make_plan(sg_engine *e)
             if (s->kind != 0 && s->begin == 0 && s->end == e->n) fully[p]++;
         }
         if ((s->kind == SG_BUILTIN_SIR_A || s->kind == SG_BUILTIN_SIR_B) &&
-            s->bp.strategy == SG_SIR_COUNT)
+            s->bp.strategy != SG_SIR_PULL)
             pl.count_step = s;
     }
     pl.count_inplace = pl.count_step != nullptr && pl.order.size() == 1;
+    pl.frontier = pl.count_step != nullptr && pl.count_step->bp.strategy == SG_SIR_FRONTIER;
     for (size_t p = 0; p < e->props.size(); ++p) {
         if (!written[p]) continue;
         if (pl.count_inplace && (int32_t)p == pl.count_step->bp.state_prop) continue;
@@ -566,6 +570,14 @@ static SgTickArgs base_args(sg_engine *e, SgStep *s, int32_t r, bool inplace)
     const bool sym = (e->graph_flags & SG_GRAPH_SYMMETRIC) != 0;
     a.toff = sym ? e->off.as<int32_t>() : e->toff.as<int32_t>();
     a.tidx = sym ? e->idx.as<int32_t>() : e->tidx.as<int32_t>();
+    a.list[0] = e->flist[0].as<int32_t>();
+    a.list[1] = e->flist[1].as<int32_t>();
+    a.list_len = e->flen.as<int32_t>();
+    a.nch = e->fnch.as<int32_t>();
+    a.mark = e->fmark.as<int32_t>();
+    a.aseg = nullptr;
+    a.stats_init = e->fstats_init.as<unsigned long long>();
+    a.stats_delta = e->fstats_delta.as<unsigned long long>();
     return a;
 }
 
@@ -590,6 +602,27 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
                          bool capturing)
 {
     const int grid_sc = e->sm_count * 4;
+    if (pl.frontier) {
+        SgStep *s = pl.count_step;
+        SgTickArgs a = base_args(e, s, 0, true);
+        const int variant = s->kind == SG_BUILTIN_SIR_A ? 1 : 2;
+        const int fgrid = e->sm_count * 8;
+        SG_CK(cudaMemsetAsync(e->flen.p, 0, (size_t)(nticks + 1) * 4, e->stream));
+        SG_CK(cudaMemsetAsync(e->fnch.p, 0, (size_t)std::max(nticks, 1) * 4, e->stream));
+        if (stats_on) {
+            SG_CK(cudaMemsetAsync(e->fstats_init.p, 0, 4 * 8, e->stream));
+            SG_CK(cudaMemsetAsync(e->fstats_delta.p, 0, (size_t)std::max(nticks, 1) * 32, e->stream));
+        }
+        SG_PROF_LAUNCH("sir_count_init",
+                       sg_launch_sir_count_init(a, grid_for(e, s->ntiles) + a.mega_blocks, e->stream));
+        SG_PROF_LAUNCH("frontier_build", sg_launch_frontier_build(a, stats_on, grid_for(e, s->ntiles), e->stream));
+        for (int32_t r = 0; r < nticks; ++r) {
+            a.r = r;
+            SG_PROF_LAUNCH("frontier_step", sg_launch_frontier_step(a, variant, stats_on, fgrid, e->stream));
+            SG_PROF_LAUNCH("frontier_scatter", sg_launch_frontier_scatter(a, fgrid, e->stream));
+        }
+        return SG_OK;
+    }
     if (pl.count_step) {
         SgStep *s = pl.count_step;
         SgTickArgs a = base_args(e, s, 0, pl.count_inplace);
@@ -668,6 +701,18 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
         SG_CK(e->cnt.reserve((size_t)std::max<int64_t>(e->n, 1) * 4));
         SG_CK(e->changes.reserve((size_t)std::max<int64_t>(e->n, 1) * 4));
     }
+    if (pl.frontier) {
+        if (!pl.count_inplace)
+            return e->fail(SG_ERR_INVALID, "the frontier strategy needs the SIR step to be the engine's only step");
+        const size_t nb = (size_t)std::max<int64_t>(e->n, 1) * 4;
+        SG_CK(e->flist[0].reserve(nb));
+        SG_CK(e->flist[1].reserve(nb));
+        SG_CK(e->fmark.reserve(nb));
+        SG_CK(e->flen.reserve((size_t)(nticks + 1) * 4));
+        SG_CK(e->fnch.reserve((size_t)std::max(nticks, 1) * 4));
+        SG_CK(e->fstats_init.reserve(4 * 8));
+        SG_CK(e->fstats_delta.reserve((size_t)std::max(nticks, 1) * 32));
+    }
     {
         // property views of compiled steps; cur0 fixes the parity at r == 0
         std::vector<sg_prop_dev> tab;
@@ -690,6 +735,7 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
 
 static void finish_run(sg_engine *e, const SgPlan &pl, int32_t nticks)
 {
+    e->last_nticks = nticks;
     for (int32_t p : pl.swap_props) e->props[p]->cur = (e->props[p]->cur + nticks) & 1;
 }
 
@@ -725,7 +771,28 @@ int sg_run(sg_engine *e, int64_t tick0, int32_t nticks, int64_t *tick_stats, sg_
     std::vector<unsigned long long> st;
     if (stats_on && nticks > 0) {
         st.resize((size_t)nticks * 4);
-        SG_CK(cudaMemcpy(st.data(), e->stats.p, st.size() * 8, cudaMemcpyDeviceToHost));
+        if (pl.frontier) {
+            // deltas per tick -> absolute S, I, R after the tick and E_S at its start
+            unsigned long long init[4];
+            std::vector<unsigned long long> d((size_t)nticks * 4);
+            SG_CK(cudaMemcpy(init, e->fstats_init.p, sizeof init, cudaMemcpyDeviceToHost));
+            SG_CK(cudaMemcpy(d.data(), e->fstats_delta.p, d.size() * 8, cudaMemcpyDeviceToHost));
+            unsigned long long S = init[0], I = init[1], R = init[2], ES = init[3];
+            for (int32_t r = 0; r < nticks; ++r) {
+                const unsigned long long inf = d[(size_t)r * 4], rec = d[(size_t)r * 4 + 1],
+                                         deg = d[(size_t)r * 4 + 2];
+                st[(size_t)r * 4 + 3] = ES;
+                S -= inf;
+                I = I + inf - rec;
+                R += rec;
+                ES -= deg;
+                st[(size_t)r * 4] = S;
+                st[(size_t)r * 4 + 1] = I;
+                st[(size_t)r * 4 + 2] = R;
+            }
+        } else {
+            SG_CK(cudaMemcpy(st.data(), e->stats.p, st.size() * 8, cudaMemcpyDeviceToHost));
+        }
         if (tick_stats)
             for (size_t k = 0; k < st.size(); ++k) tick_stats[k] = (int64_t)st[k];
     }
@@ -782,6 +849,26 @@ int sg_run_async(sg_engine *e, int64_t tick0, int32_t nticks, int32_t use_graph)
     }
     SG_CK(cudaGraphLaunch(e->graph_exec, e->stream));
     finish_run(e, pl, nticks);
+    return SG_OK;
+}
+
+int sg_last_run_active(sg_engine *e, int64_t *out, int32_t n)
+{
+    if (!e || (n > 0 && !out) || n < 0) return SG_ERR_INVALID;
+    cudaSetDevice(e->device);
+    SG_CK(cudaStreamSynchronize(e->stream));
+    SgPlan pl = make_plan(e);
+    if (pl.frontier) {
+        if (n > e->last_nticks) return e->fail(SG_ERR_INVALID, "n exceeds the last run's ticks");
+        std::vector<int32_t> len((size_t)n);
+        if (n) SG_CK(cudaMemcpy(len.data(), e->flen.p, (size_t)n * 4, cudaMemcpyDeviceToHost));
+        for (int32_t r = 0; r < n; ++r) out[r] = len[(size_t)r];
+        return SG_OK;
+    }
+    int64_t agents = 0;
+    for (SgStep *s : pl.order)
+        if (s->kind == SG_BUILTIN_SIR_A || s->kind == SG_BUILTIN_SIR_B) agents += s->end - s->begin;
+    for (int32_t r = 0; r < n; ++r) out[r] = agents;
     return SG_OK;
 }
 

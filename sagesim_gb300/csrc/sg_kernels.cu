@@ -165,6 +165,40 @@ __device__ __forceinline__ bool warp_draws(uint32_t j0, int c, uint32_t c0b, uin
     return false;
 }
 
+// SIR-B outcome for every lane's agent given its infected-neighbour count k
+// (act = the lane has a susceptible agent with k > 0). Each lane tests its
+// first kLaneDraws draws itself; agents that need more share the warp, which
+// tests 32 draws (salt 2 + j) per step. Every lane of the warp must call it.
+constexpr int32_t kLaneDraws = 2;
+
+__device__ __forceinline__ bool sirb_infected(bool act, int32_t k, uint32_t c0b, uint32_t lid,
+                                              uint32_t key, uint32_t kinf, int lane)
+{
+    bool inf = false;
+    int32_t done = 0;
+    if (act) {
+        done = k < kLaneDraws ? k : kLaneDraws;
+        for (int32_t j = 0; j < done; ++j)
+            if (sg_philox_k23(c0b + 2u + (uint32_t)j, lid, key) < kinf) {
+                inf = true;
+                break;
+            }
+    }
+    unsigned m = __ballot_sync(FULL_MASK, act && !inf && k > done);
+    while (m) {
+        const int l = __ffs(m) - 1;
+        m &= m - 1;
+        const int32_t bk = __shfl_sync(FULL_MASK, k, l);
+        const uint32_t bc = __shfl_sync(FULL_MASK, c0b, l);
+        const uint32_t bl = __shfl_sync(FULL_MASK, lid, l);
+        const uint32_t bkey = __shfl_sync(FULL_MASK, key, l);
+        const uint32_t bkinf = __shfl_sync(FULL_MASK, kinf, l);
+        const bool hit = warp_draws((uint32_t)kLaneDraws, bk - kLaneDraws, bc, bl, bkey, bkinf, lane);
+        if (lane == l) inf = hit;
+    }
+    return inf;
+}
+
 // VARIANT 1: any infected; 2: SIR-B trials; 0: count (returned through *count).
 template <int VARIANT>
 __device__ __forceinline__ bool warp_row(const int32_t *__restrict__ idx,
@@ -547,6 +581,240 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_scatter_kernel(SgTic
     }
 }
 
+// ---- frontier strategy ------------------------------------------------------------
+// Only "active" agents can change: infected agents (recovery draw) and
+// susceptible agents with at least one infected neighbour (cnt > 0). The
+// frontier strategy keeps them in a compact list per tick, so a tick costs
+// O(active + edges of changed agents) instead of O(agents):
+//   build  (run start) list[0] = {I} U {S with cnt > 0}; mark[i] = 0 for them
+//   step r   each listed agent draws; it stays listed (mark = r+1, appended to
+//            list r+1) while it is I or S with cnt > 0; S->I and I->R changes go
+//            to the change list of tick r
+//   scatter r  +-1 along the transpose rows of the changes; a susceptible agent
+//            whose count goes 0 -> 1 joins list r+1 unless mark[] says it is
+//            already there (atomicExch on mark deduplicates)
+// State is updated in place (only listed agents are touched), and the draws
+// are the same as in the count strategy, so results are bit-identical.
+
+// All threads of the block call it: appends `value` for every thread whose
+// flag is set, one global atomic per block.
+__device__ __forceinline__ void block_append(bool flag, int32_t value, int32_t *__restrict__ list,
+                                             int32_t *counter, int32_t *sh /* kWarps + 1 */)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned m = __ballot_sync(FULL_MASK, flag);
+    if (lane == 0) sh[warp] = __popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int32_t total = 0;
+        for (int w = 0; w < kWarps; ++w) {
+            const int32_t c = sh[w];
+            sh[w] = total;
+            total += c;
+        }
+        sh[kWarps] = total ? atomicAdd(counter, total) : 0;
+    }
+    __syncthreads();
+    if (flag) list[sh[kWarps] + sh[warp] + __popc(m & ((1u << lane) - 1u))] = value;
+    __syncthreads();
+}
+
+__device__ __forceinline__ const SgSeg &seg_of(const SgTickArgs &a, int32_t agent)
+{
+    return a.segs[a.aseg ? __ldg(a.aseg + agent) : 0];
+}
+
+// list[0] and mark[] from the tiles; with STATS also the initial S/I/R/E_S totals.
+template <bool STATS>
+__global__ void __launch_bounds__(SG_SIR_THREADS) frontier_build_kernel(SgTickArgs a)
+{
+    __shared__ int32_t sh[kWarps + 1];
+    __shared__ unsigned long long red[4][kWarps];
+    const int tid = threadIdx.x;
+    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+        const SgTile tile = a.tiles[t];
+        const SgSeg &sg = a.segs[tile.seg];
+        const int32_t *st = (const int32_t *)a.buf0;
+        unsigned long long nS = 0, nI = 0, nR = 0, eS = 0;
+        for (int32_t base = tile.begin; base < tile.end; base += SG_SIR_THREADS) {
+            const int32_t i = base + tid;
+            bool in = false;
+            if (i < tile.end) {
+                const int32_t s = st[i];
+                in = (s == sg.ci) || (s == sg.cs && a.cnt[i] > 0);
+                a.mark[i] = in ? 0 : -1;
+                if (STATS) {
+                    nS += (s == sg.cs);
+                    nI += (s == sg.ci);
+                    nR += (s == sg.cr);
+                    if (s == sg.cs) eS += (unsigned long long)(a.off[i + 1] - a.off[i]);
+                }
+            }
+            block_append(in, i, a.list[0], a.list_len, sh);
+        }
+        if (STATS && sg.stats) block_flush4(nS, nI, nR, eS, a.stats_init, red);
+    }
+}
+
+// STATS rows are deltas: infections, recoveries, sum of the infected agents'
+// degrees (the engine turns them into absolute S/I/R/E_S per tick).
+template <int VARIANT, bool STATS>
+__global__ void __launch_bounds__(SG_SIR_THREADS) frontier_step_kernel(SgTickArgs a)
+{
+    __shared__ int32_t sh[kWarps + 1];
+    __shared__ unsigned long long red[4][kWarps];
+    constexpr int U = 4;
+    const int tid = threadIdx.x;
+    const int32_t n = a.list_len[a.r];
+    const int32_t *__restrict__ lin = a.list[a.r & 1];
+    int32_t *__restrict__ lout = a.list[(a.r + 1) & 1];
+    int32_t *st = (int32_t *)a.buf0;
+    unsigned long long dInf = 0, dRec = 0, dDeg = 0;
+    for (int32_t base = blockIdx.x * (SG_SIR_THREADS * U); base < n; base += gridDim.x * (SG_SIR_THREADS * U)) {
+        int32_t ag[U], s[U], k[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int32_t q = base + u * SG_SIR_THREADS + tid;
+            ag[u] = q < n ? lin[q] : -1;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) s[u] = ag[u] >= 0 ? st[ag[u]] : INT32_MIN;
+#pragma unroll
+        for (int u = 0; u < U; ++u) k[u] = ag[u] >= 0 ? a.cnt[ag[u]] : 0;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            bool keep = false, chg = false, sus = false;
+            int32_t code = 0, sci = 0;
+            uint32_t slid = 0, sc0b = 0, skey = 0, skinf = 0;
+            if (ag[u] >= 0) {
+                const int32_t i = ag[u];
+                const SgSeg &sg = seg_of(a, i);
+                const int64_t tick = sg.tick0 + a.r;
+                if (tick < sg.end_tick) {
+                    const uint32_t c0b = sg_c0base(tick);
+                    if (s[u] == sg.ci) {
+                        if (sg_philox_k23(c0b + 1u, seg_lid(sg, i), sg.key) < sg.krec) {
+                            st[i] = sg.cr;
+                            chg = true;
+                            code = ~i;
+                            if (STATS) ++dRec;
+                        } else {
+                            keep = true;
+                        }
+                    } else if (s[u] == sg.cs && k[u] > 0) {
+                        sus = true;
+                        keep = true;
+                        slid = seg_lid(sg, i);
+                        sc0b = c0b;
+                        skey = sg.key;
+                        skinf = sg.kinf;
+                        sci = sg.ci;
+                    }
+                    if (keep) a.mark[i] = a.r + 1;
+                }
+            }
+            // susceptible agents with infected neighbours: the draws
+            bool inf;
+            if (VARIANT == 1)
+                inf = sus && sg_philox_k23(sc0b + 1u, slid, skey) < skinf;
+            else
+                inf = sirb_infected(sus, k[u], sc0b, slid, skey, skinf, tid & 31);
+            if (inf) {
+                const int32_t i = ag[u];
+                st[i] = sci;
+                chg = true;
+                code = i;
+                if (STATS) {
+                    ++dInf;
+                    dDeg += (unsigned long long)(a.off[i + 1] - a.off[i]);
+                }
+            }
+            block_append(keep, ag[u], lout, a.list_len + a.r + 1, sh);
+            block_append(chg, code, a.changes, a.nch + a.r, sh);
+        }
+    }
+    if (STATS && a.stats_delta) block_flush4(dInf, dRec, dDeg, 0ull, a.stats_delta + 4 * (int64_t)a.r, red);
+}
+
+__global__ void __launch_bounds__(SG_SIR_THREADS) frontier_scatter_kernel(SgTickArgs a)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int32_t n = a.nch[a.r];
+    const int32_t *st = (const int32_t *)a.buf0;
+    int32_t *lout = a.list[(a.r + 1) & 1];
+    int32_t *len = a.list_len + a.r + 1;
+    const int32_t next = a.r + 1;
+    const int32_t trow = thread_row_of(a);
+    for (int32_t q0 = (blockIdx.x * kWarps + warp) * 32; q0 < n; q0 += gridDim.x * kWarps * 32) {
+        const int32_t q = q0 + lane;
+        const bool valid = q < n;
+        const int32_t c = valid ? a.changes[q] : 0;
+        const int32_t g = c >= 0 ? c : ~c;
+        const int32_t delta = c >= 0 ? 1 : -1;
+        int32_t b = 0, e = 0, cs = 0;
+        if (valid) {
+            b = __ldg(a.toff + g);
+            e = __ldg(a.toff + g + 1);
+            cs = seg_of(a, g).cs;
+        }
+        const bool long_row = e - b > trow;
+        // candidates (count 0 -> 1, susceptible, not yet listed) are appended
+        // warp-aggregated after each batch of neighbour updates
+        for (int32_t t = 0;; ++t) { // row position t of every short row, in lockstep
+            const bool act = !long_row && b + t < e;
+            if (!__any_sync(FULL_MASK, act)) break;
+            bool cand = false;
+            int32_t p = 0;
+            if (act) {
+                p = __ldg(a.tidx + b + t);
+                if (delta < 0)
+                    atomicSub(a.cnt + p, 1);
+                else
+                    cand = atomicAdd(a.cnt + p, 1) == 0 && st[p] == cs &&
+                           atomicExch(a.mark + p, next) != next;
+            }
+            const unsigned cm = __ballot_sync(FULL_MASK, cand);
+            if (cm) {
+                const int leader = __ffs(cm) - 1;
+                int32_t pos = 0;
+                if (lane == leader) pos = atomicAdd(len, __popc(cm));
+                pos = __shfl_sync(FULL_MASK, pos, leader);
+                if (cand) lout[pos + __popc(cm & ((1u << lane) - 1u))] = p;
+            }
+        }
+        unsigned m = __ballot_sync(FULL_MASK, long_row);
+        while (m) {
+            const int l = __ffs(m) - 1;
+            m &= m - 1;
+            const int32_t hb = __shfl_sync(FULL_MASK, b, l);
+            const int32_t he = __shfl_sync(FULL_MASK, e, l);
+            const int32_t hd = __shfl_sync(FULL_MASK, delta, l);
+            const int32_t hcs = __shfl_sync(FULL_MASK, cs, l);
+            for (int32_t k0 = hb; k0 < he; k0 += 32) {
+                const int32_t k = k0 + lane;
+                bool cand = false;
+                int32_t p = 0;
+                if (k < he) {
+                    p = __ldg(a.tidx + k);
+                    if (hd < 0)
+                        atomicSub(a.cnt + p, 1);
+                    else
+                        cand = atomicAdd(a.cnt + p, 1) == 0 && st[p] == hcs &&
+                               atomicExch(a.mark + p, next) != next;
+                }
+                const unsigned cm = __ballot_sync(FULL_MASK, cand);
+                if (cm) {
+                    const int leader = __ffs(cm) - 1;
+                    int32_t pos = 0;
+                    if (lane == leader) pos = atomicAdd(len, __popc(cm));
+                    pos = __shfl_sync(FULL_MASK, pos, leader);
+                    if (cand) lout[pos + __popc(cm & ((1u << lane) - 1u))] = p;
+                }
+            }
+        }
+    }
+}
+
 // ---- opinion model --------------------------------------------------------------
 // x' = clamp((double)(sum_j w_j x_nbr_j / sum_j |w_j|) + sigma * N(0,1), 0, 1)
 // over the first min(deg, width) ordered neighbours; float32 sums in row order
@@ -721,4 +989,35 @@ cudaError_t sg_transpose_csr(const int32_t *off, const int32_t *idx, int64_t n, 
         err = cudaGetLastError();
     }
     return err;
+}
+
+cudaError_t sg_launch_frontier_build(const SgTickArgs &a, bool stats, int grid, cudaStream_t st)
+{
+    if (stats)
+        frontier_build_kernel<true><<<grid, SG_SIR_THREADS, 0, st>>>(a);
+    else
+        frontier_build_kernel<false><<<grid, SG_SIR_THREADS, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_launch_frontier_step(const SgTickArgs &a, int variant, bool stats, int grid, cudaStream_t st)
+{
+    if (variant == 1) {
+        if (stats)
+            frontier_step_kernel<1, true><<<grid, SG_SIR_THREADS, 0, st>>>(a);
+        else
+            frontier_step_kernel<1, false><<<grid, SG_SIR_THREADS, 0, st>>>(a);
+    } else {
+        if (stats)
+            frontier_step_kernel<2, true><<<grid, SG_SIR_THREADS, 0, st>>>(a);
+        else
+            frontier_step_kernel<2, false><<<grid, SG_SIR_THREADS, 0, st>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t sg_launch_frontier_scatter(const SgTickArgs &a, int grid, cudaStream_t st)
+{
+    frontier_scatter_kernel<<<grid, SG_SIR_THREADS, 0, st>>>(a);
+    return cudaGetLastError();
 }

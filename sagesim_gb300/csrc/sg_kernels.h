@@ -60,6 +60,14 @@ struct SgTickArgs {
     int32_t *tile_nch;      // [ntiles] changes recorded by each tile this tick
     const int32_t *toff;    // transpose CSR (in-neighbours)
     const int32_t *tidx;
+    // frontier strategy
+    int32_t *list[2];       // active agents of tick r in list[r & 1]
+    int32_t *list_len;      // [ticks + 1] list lengths, slot r
+    int32_t *nch;           // [ticks] change counts, slot r (changes[] reused per tick)
+    int32_t *mark;          // per agent: the last list index it was appended to
+    const int32_t *aseg;    // per agent: its segment (NULL = segment 0)
+    unsigned long long *stats_init;  // build: S, I, R, E_S at the run start
+    unsigned long long *stats_delta; // step: [ticks][4] infections, recoveries, degree sum
 };
 
 // Launchers return cudaGetLastError() of the launch.
@@ -75,6 +83,11 @@ cudaError_t sg_launch_sir_count_init(const SgTickArgs &a, int grid, cudaStream_t
 cudaError_t sg_launch_sir_count_step(const SgTickArgs &a, int variant, bool stats, bool inplace,
                                      int grid, cudaStream_t st);
 cudaError_t sg_launch_sir_count_scatter(const SgTickArgs &a, int grid, cudaStream_t st);
+// Frontier strategy (state in buf0, updated in place). list_len[0..ticks] and
+// nch[0..ticks-1] must be zero before the build.
+cudaError_t sg_launch_frontier_build(const SgTickArgs &a, bool stats, int grid, cudaStream_t st);
+cudaError_t sg_launch_frontier_step(const SgTickArgs &a, int variant, bool stats, int grid, cudaStream_t st);
+cudaError_t sg_launch_frontier_scatter(const SgTickArgs &a, int grid, cudaStream_t st);
 cudaError_t sg_launch_opinion(const SgTickArgs &a, int grid, cudaStream_t st);
 // Copies [begin, end) of `words` 32-bit words from src to dst (write-back of
 // agents outside a step's range).

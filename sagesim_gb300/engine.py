@@ -119,7 +119,7 @@ class Engine:
     @staticmethod
     def _params(builtin, state_prop, begin, end, beta=0.0, gamma=0.0, codes=(1, 2, 3),
                 strategy="count", priority=0, aux_prop=-1, sigma=0.0):
-        st = {"pull": N.SG_SIR_PULL, "count": N.SG_SIR_COUNT}[strategy]
+        st = {"pull": N.SG_SIR_PULL, "count": N.SG_SIR_COUNT, "frontier": N.SG_SIR_FRONTIER}[strategy]
         return N.BuiltinParams(builtin, st, state_prop, aux_prop, codes[0], codes[1], codes[2],
                                priority, int(begin), int(end), float(beta), float(gamma), float(sigma))
 
@@ -165,6 +165,11 @@ class Engine:
 
     def run_async(self, tick0, nticks, use_graph=True):
         self._ck(self._lib.sg_run_async(self._h, int(tick0), int(nticks), 1 if use_graph else 0))
+
+    def last_run_active(self, nticks):
+        out = np.zeros(nticks, dtype=np.int64)
+        self._ck(self._lib.sg_last_run_active(self._h, _ptr(out), int(nticks)))
+        return out
 
     def synchronize(self):
         self._ck(self._lib.sg_synchronize(self._h))

@@ -251,7 +251,14 @@ class Model:
         for priority, bidx, fn, _ in self._steps:
             b, en = self._breed_ranges[bidx]
             if isinstance(fn, SIRStep):
-                strategy = fn.strategy or ("count" if len(writers.get(fn.state, [])) == 1 else "pull")
+                if fn.strategy:
+                    strategy = fn.strategy
+                elif len(self._steps) == 1:
+                    strategy = "frontier"  # the only step: active-list ticks, state in place
+                elif len(writers.get(fn.state, [])) == 1:
+                    strategy = "count"
+                else:
+                    strategy = "pull"
                 sid = e.add_sir(self._pid[fn.state], self._scalar_global(fn.p_infection),
                                 self._scalar_global(fn.p_recovery), variant=fn.variant, strategy=strategy,
                                 codes=fn.codes, begin=b, end=en, priority=priority)

@@ -27,8 +27,8 @@ class SIRStep:
                  p_recovery="p_recovery", codes=(1, 2, 3), strategy=None):
         if variant not in ("A", "B"):
             raise ValueError("variant must be 'A' or 'B'")
-        if strategy not in (None, "count", "pull"):
-            raise ValueError("strategy must be None, 'count' or 'pull'")
+        if strategy not in (None, "count", "pull", "frontier"):
+            raise ValueError("strategy must be None, 'count', 'pull' or 'frontier'")
         self.variant = variant
         self.state = state
         self.p_infection = p_infection

@@ -43,7 +43,7 @@ def hub_graph(seed=3):
 
 
 @pytest.mark.parametrize("variant", ["A", "B"])
-@pytest.mark.parametrize("strategy", ["pull", "count"])
+@pytest.mark.parametrize("strategy", ["pull", "count", "frontier"])
 @pytest.mark.parametrize("kind", ["er", "ba", "hubs", "directed"])
 def test_sir_matches_oracle_every_tick(variant, strategy, kind):
     if kind == "er":

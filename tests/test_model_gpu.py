@@ -66,7 +66,7 @@ def test_deterministic_sir_chain_known_answer():
                                                  ("sto20_seed999", 20, (0.5, 0.3), 999, 10),
                                                  ("sto50_seed111", 50, (0.3, 0.2), 111, 20),
                                                  ("sto50_seed222", 50, (0.3, 0.2), 222, 20)])
-@pytest.mark.parametrize("strategy", ["count", "pull"])
+@pytest.mark.parametrize("strategy", ["count", "pull", "frontier"])
 def test_chain_every_tick_matches_reference(key, n, p, seed, ticks, strategy):
     hist = gold("chain.npz")[key]
     m = chain_model(n, p[0], p[1], seed, SIRStep("A", strategy=strategy))
@@ -192,7 +192,7 @@ def er_model(step, d, seed=0):
 
 
 @pytest.mark.parametrize("variant,key", [("A", "sir_a"), ("B", "sir_b")])
-@pytest.mark.parametrize("strategy", ["count", "pull"])
+@pytest.mark.parametrize("strategy", ["count", "pull", "frontier"])
 def test_er_10k_every_tick_matches_reference(variant, key, strategy):
     """10,000-agent ER (p=0.001, seed 0), 1 % infected, 100 ticks."""
     d = gold("er_c1.npz")
