@@ -125,6 +125,163 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def ensemble_specs(count=512, seed=3):
+    """Config 4: n log-uniform in [1e3, 1e6]; ER (mean degree 8), BA (m 3..6) or
+    WS (k 6..12, p 0.1); beta U[0.01, 0.1], gamma U[0.05, 0.2]; 0.5 % infected."""
+    rng = np.random.default_rng(seed)
+    specs, params = [], []
+    for s_ in range(count):
+        n = int(10 ** rng.uniform(3, 6))
+        kind = int(rng.integers(0, 3))
+        gseed = int(rng.integers(0, 2**62))
+        if kind == 0:
+            specs.append(("er", n, 8.0 / (n - 1), gseed))
+        elif kind == 1:
+            specs.append(("ba", n, int(rng.integers(3, 7)), gseed))
+        else:
+            specs.append(("ws", n, int(rng.choice([6, 8, 10, 12])), 0.1, gseed))
+        params.append(dict(seed=int(rng.integers(0, 2**31)), beta=float(rng.uniform(0.01, 0.1)),
+                           gamma=float(rng.uniform(0.05, 0.2)), infected_seed=int(rng.integers(0, 2**31))))
+    return specs, params
+
+
+def initial_state(n, frac, seed):
+    st = np.full(n, CODES[0], dtype=np.int32)
+    k = max(1, int(round(frac * n)))
+    st[np.random.default_rng(seed).choice(n, size=k, replace=False)] = CODES[1]
+    return st
+
+
+def ensemble_section(stream, steps, device=0, ticks=365):
+    """Batched ensemble vs the same scenarios run one after another on the plain
+    engine (device time of the simulate() calls only), bit-exact compared."""
+    import torch
+
+    from sagesim_gb300 import Engine, graphs
+    from sagesim_gb300.batch import Batch
+
+    specs, params = ensemble_specs()
+    t0 = time.perf_counter()
+    gs = graphs.generate_many(specs)
+    gen_s = time.perf_counter() - t0
+    states = [initial_state(off.size - 1, 0.005, p["infected_seed"]) for (off, _), p in zip(gs, params)]
+    agents = sum(off.size - 1 for off, _ in gs)
+    nnz = sum(int(off[-1]) for off, _ in gs)
+    with torch.cuda.stream(stream):
+        b = Batch(device=device, stream=stream.cuda_stream)
+        sids = [b.add_scenario(off, idx, st, p["seed"], p["beta"], p["gamma"], variant="B", horizon=ticks)
+                for (off, idx), st, p in zip(gs, states, params)]
+        b.commit()
+        b.snapshot()
+        tune = b.tune(4)
+        b.restore()
+        b.run(ticks)  # warm-up (graph capture)
+        b.restore()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        stream.synchronize()
+        ms_total = 0.0
+        for _ in range(steps):
+            b.restore()
+            ev0.record(stream)
+            b.run(ticks)
+            ev1.record(stream)
+            stream.synchronize()
+            ms_total += ev0.elapsed_time(ev1)
+        batched_ms = ms_total / steps
+        finals = [b.get_state(sid) for sid in sids]
+        info = b.info()
+        b.close()
+        # the same scenarios on the plain engine, one after another
+        plain_ms = 0.0
+        mismatches = 0
+        for (off, idx), st, p, fin in zip(gs, states, params, finals):
+            e = Engine(device=device, stream=stream.cuda_stream)
+            e.set_graph(off, idx, symmetric=True)
+            e.set_seed(p["seed"])
+            pr = e.add_property("state", np.int32, init=st)
+            e.add_sir(pr, p["beta"], p["gamma"], variant="B", strategy="count", codes=CODES)
+            e.snapshot()
+            e.run_async(0, ticks)  # warm-up (graph capture)
+            e.restore()
+            stream.synchronize()
+            ev0.record(stream)
+            e.run_async(0, ticks)
+            ev1.record(stream)
+            stream.synchronize()
+            plain_ms += ev0.elapsed_time(ev1)
+            mismatches += int(not np.array_equal(e.get_property(pr), fin))
+            e.close()
+    return {"workload": "512 SIR scenarios (ER/BA/WS, n log-uniform 1e3..1e6, seed 3), 365 ticks",
+            "scenarios": len(gs), "agents": agents, "nnz": nnz, "graph_gen_s": gen_s,
+            "batched_agent_ticks_per_s": agents * ticks / (batched_ms / 1e3), "batched_ms": batched_ms,
+            "plain_sequential_agent_ticks_per_s": agents * ticks / (plain_ms / 1e3),
+            "plain_sequential_ms": plain_ms, "speedup": plain_ms / batched_ms,
+            "tune": tune, "bit_exact_scenarios": len(gs) - mismatches, "device_bytes": info["device_bytes"]}
+
+
+def serving_section(stream, device=0, n_requests=100, n_graphs=24):
+    """Config 5 scaled to n_requests: Poisson arrivals at 200 req/s (seed 4),
+    n log-uniform in [1e4, 5e6], BA or ER with mean degree 4..16, horizons
+    U{50..365}, 150 GB admission budget. Graph structures come from a pool of
+    n_graphs generated graphs; every request has its own seed, beta, gamma,
+    initial infections and horizon."""
+    import torch
+
+    from sagesim_gb300 import Engine, graphs
+    from sagesim_gb300.serve import Server, serve_stream
+
+    rng = np.random.default_rng(4)
+    specs = []
+    for g in range(n_graphs):
+        n = int(10 ** rng.uniform(4, np.log10(5e6)))
+        deg = float(rng.uniform(4, 16))
+        if rng.random() < 0.5:
+            specs.append(("ba", n, max(2, int(round(deg / 2))), int(rng.integers(0, 2**62))))
+        else:
+            specs.append(("er", n, deg / (n - 1), int(rng.integers(0, 2**62))))
+    gs = graphs.generate_many(specs)
+    arrivals = np.cumsum(rng.exponential(1.0 / 200.0, size=n_requests))
+    reqs = []
+    for i in range(n_requests):
+        off, idx = gs[int(rng.integers(0, n_graphs))]
+        n = off.size - 1
+        reqs.append(dict(offsets=off, indices=idx, state=initial_state(n, 0.005, int(rng.integers(0, 2**31))),
+                         seed=int(rng.integers(0, 2**31)), beta=float(rng.uniform(0.01, 0.1)),
+                         gamma=float(rng.uniform(0.05, 0.2)), horizon=int(rng.integers(50, 366))))
+    with torch.cuda.stream(stream):
+        srv = Server(budget_bytes=150 * 10**9, agent_slots=400_000_000, edge_slots=2_100_000_000,
+                     max_resident=4096, variant="B", device=device, stream=stream.cuda_stream)
+        out = serve_stream(srv, reqs, arrivals, chunk=8)
+        srv.close()
+        # plain sequential: each request alone on the plain engine (device time)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        plain_ms, mismatches, checked = 0.0, 0, 0
+        for i, r in enumerate(reqs):
+            e = Engine(device=device, stream=stream.cuda_stream)
+            e.set_graph(r["offsets"], r["indices"], symmetric=True)
+            e.set_seed(r["seed"])
+            pr = e.add_property("state", np.int32, init=r["state"])
+            e.add_sir(pr, r["beta"], r["gamma"], variant="B", strategy="count", codes=CODES)
+            stream.synchronize()
+            ev0.record(stream)
+            e.run_async(0, r["horizon"], use_graph=False)
+            ev1.record(stream)
+            stream.synchronize()
+            plain_ms += ev0.elapsed_time(ev1)
+            mismatches += int(not np.array_equal(e.get_property(pr), out["results"][i]))
+            checked += 1
+            e.close()
+    lat = out["latency_s"]
+    agent_ticks = out["agent_ticks"]
+    return {"workload": "%d SIR requests, Poisson 200 req/s (seed 4), n 1e4..5e6 log-uniform, BA/ER "
+                        "mean degree 4..16, horizons 50..365, 150 GB budget, %d graph structures"
+                        % (n_requests, n_graphs),
+            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "served_agent_ticks_per_s": agent_ticks / out["wall_s"], "wall_s": out["wall_s"],
+            "plain_sequential_agent_ticks_per_s": agent_ticks / (plain_ms / 1e3),
+            "bit_exact_requests": checked - mismatches, "requests": n_requests}
+
+
 def algorithmic_bytes(kernel, n, st0, tick_stats, active):
     """Compulsory DRAM bytes per launch of `kernel`, per tick of the run (int32 state).
 
@@ -233,6 +390,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--strategy", default="count", choices=["count", "frontier", "pull"])
     ap.add_argument("--agents", type=int, default=N_AGENTS)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the ensemble and serving sections")
     ap.add_argument("--profile-case", action="store_true",
                     help="run one simulate(200) of --strategy and exit (for ncu captures)")
     args = ap.parse_args()
@@ -357,6 +516,15 @@ def main():
         if not np.array_equal(r_["final"], head["final"]):
             raise RuntimeError("strategies disagree on the final state")
 
+    extra = {}
+    if rank == 0 and not args.no_extras:
+        for name, fn in (("ensemble", lambda: ensemble_section(stream, max(1, min(args.steps, 3)), local)),
+                         ("serving", lambda: serving_section(stream, local))):
+            try:
+                extra[name] = fn()
+            except Exception as exc:  # a failing extra section must not lose the headline line
+                extra[name] = {"error": "%s: %s" % (type(exc).__name__, exc)}
+
     cpu = None
     if rank == 0:
         sample = max(1, _env_int("SG_CPU_TICKS", 10))
@@ -387,6 +555,7 @@ def main():
         "strategies": {k: {kk: vv for kk, vv in v.items() if kk not in ("final", "clocks")}
                        for k, v in results.items()},
     }
+    line.update(extra)
     if rank == 0:
         print(json.dumps(line))
     if dist:

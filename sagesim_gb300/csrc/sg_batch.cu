@@ -154,12 +154,11 @@ int SgPool::place(const sg_scenario_desc &d, const int32_t *loff, const int32_t 
         return fail(SG_ERR_BUDGET, "no room for the scenario's edges");
     }
     POOL_CK(cudaSetDevice(device));
-    std::vector<int32_t> goff((size_t)n + 1);
-    for (int64_t i = 0; i <= n; ++i) goff[(size_t)i] = (int32_t)(eb + loff[i]);
-    POOL_CK(cudaMemcpyAsync(off.as<int32_t>() + ab, goff.data(), (size_t)(n + 1) * 4, cudaMemcpyHostToDevice, stream));
-    std::vector<int32_t> gidx((size_t)nnz);
-    for (int64_t k = 0; k < nnz; ++k) gidx[(size_t)k] = (int32_t)(ab + lidx[k]);
-    if (nnz) POOL_CK(cudaMemcpyAsync(idx.as<int32_t>() + eb, gidx.data(), (size_t)nnz * 4, cudaMemcpyHostToDevice, stream));
+    // local CSR copied as is, then shifted to pool slots on the device
+    POOL_CK(cudaMemcpyAsync(off.as<int32_t>() + ab, loff, (size_t)(n + 1) * 4, cudaMemcpyHostToDevice, stream));
+    if (nnz) POOL_CK(cudaMemcpyAsync(idx.as<int32_t>() + eb, lidx, (size_t)nnz * 4, cudaMemcpyHostToDevice, stream));
+    POOL_CK(sg_launch_offset_csr(off.as<int32_t>() + ab, n + 1, (int32_t)eb, idx.as<int32_t>() + eb, nnz,
+                                 (int32_t)ab, stream));
     if (!all_symmetric) {
         // transpose rows (in-neighbours) of this scenario, placed in the same slots
         std::vector<int32_t> tcount((size_t)n + 1, 0), tcur((size_t)n);

@@ -860,6 +860,14 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) opinion_kernel(SgTickArgs a)
     }
 }
 
+__global__ void offset_csr_kernel(int32_t *__restrict__ off, int64_t n1, int32_t edge_base,
+                                  int32_t *__restrict__ idx, int64_t nnz, int32_t agent_base)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n1; i += stride) off[i] += edge_base;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz; k += stride) idx[k] += agent_base;
+}
+
 __global__ void copy_words_kernel(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
                                   int64_t n)
 {
@@ -944,6 +952,17 @@ cudaError_t sg_launch_sir_count_scatter(const SgTickArgs &a, int grid, cudaStrea
 cudaError_t sg_launch_opinion(const SgTickArgs &a, int grid, cudaStream_t st)
 {
     opinion_kernel<<<grid, SG_SIR_THREADS, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_launch_offset_csr(int32_t *off, int64_t n1, int32_t edge_base, int32_t *idx, int64_t nnz,
+                                 int32_t agent_base, cudaStream_t st)
+{
+    const int64_t work = n1 > nnz ? n1 : nnz;
+    if (work <= 0) return cudaSuccess;
+    int64_t blocks = (work + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    offset_csr_kernel<<<(int)blocks, 256, 0, st>>>(off, n1, edge_base, idx, nnz, agent_base);
     return cudaGetLastError();
 }
 

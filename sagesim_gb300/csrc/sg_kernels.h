@@ -89,6 +89,10 @@ cudaError_t sg_launch_frontier_build(const SgTickArgs &a, bool stats, int grid, 
 cudaError_t sg_launch_frontier_step(const SgTickArgs &a, int variant, bool stats, int grid, cudaStream_t st);
 cudaError_t sg_launch_frontier_scatter(const SgTickArgs &a, int grid, cudaStream_t st);
 cudaError_t sg_launch_opinion(const SgTickArgs &a, int grid, cudaStream_t st);
+// Adds edge_base to off[0..n1) and agent_base to idx[0..nnz) in place (placing a
+// scenario's local CSR into a pool).
+cudaError_t sg_launch_offset_csr(int32_t *off, int64_t n1, int32_t edge_base, int32_t *idx, int64_t nnz,
+                                 int32_t agent_base, cudaStream_t st);
 // Copies [begin, end) of `words` 32-bit words from src to dst (write-back of
 // agents outside a step's range).
 cudaError_t sg_launch_copy_words(const uint32_t *src, uint32_t *dst, int64_t n, cudaStream_t st);

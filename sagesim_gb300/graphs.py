@@ -69,3 +69,31 @@ def initial_infected(n, fraction, seed):
     """Indices of round(fraction * n) distinct agents (numpy PCG64, platform independent)."""
     k = int(round(fraction * n))
     return np.sort(np.random.default_rng(seed).choice(n, size=k, replace=False)).astype(np.int64)
+
+
+def generate(spec):
+    """One graph from a spec tuple: ("er", n, p, seed) | ("ba", n, m, seed) |
+    ("ws", n, k, p, seed)."""
+    kind = spec[0]
+    if kind == "er":
+        return erdos_renyi(*spec[1:])
+    if kind == "ba":
+        return barabasi_albert(*spec[1:])
+    if kind == "ws":
+        return watts_strogatz(*spec[1:])
+    raise ValueError("unknown graph kind %r" % (kind,))
+
+
+def generate_many(specs, processes=None):
+    """Generates graphs in parallel worker processes (spawn start method, so it
+    is safe after CUDA has been initialised in the calling process)."""
+    import multiprocessing as mp
+    import os
+
+    if processes is None:
+        processes = min(len(specs), os.cpu_count() or 1)
+    if processes <= 1 or len(specs) <= 1:
+        return [generate(s) for s in specs]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(processes) as pool:
+        return pool.map(generate, specs, chunksize=1)
