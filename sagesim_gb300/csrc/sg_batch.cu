@@ -313,7 +313,7 @@ int SgPool::enqueue(int32_t nticks, bool capturing)
         cudaError_t ce;
         if (count) {
             ce = sg_launch_sir_count_step(a, variant, false, true, grid, stream);
-            if (ce == cudaSuccess) ce = sg_launch_sir_count_scatter(a, sm_count * 4, stream);
+            if (ce == cudaSuccess) ce = sg_launch_sir_count_scatter(a, sm_count * 16, stream);
         } else {
             ce = sg_launch_sir_pull(a, variant, false, grid + a.mega_blocks, stream);
         }

@@ -601,7 +601,7 @@ static int grid_for(sg_engine *e, int32_t ntiles)
 static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool stats_on,
                          bool capturing)
 {
-    const int grid_sc = e->sm_count * 4;
+    const int grid_sc = e->sm_count * 16;
     if (pl.frontier) {
         SgStep *s = pl.count_step;
         SgTickArgs a = base_args(e, s, 0, true);

@@ -437,100 +437,117 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_init_kernel(SgTickAr
 
 constexpr int kPerThread = SG_TILE / SG_SIR_THREADS; // agents per thread in a tile
 
+// Count-strategy step. The tail of an epidemic makes this a streaming pass over
+// every agent, so the kernel is built for memory-level parallelism: each
+// thread handles kCountPer agents per pass with their state, count and RNG key
+// loaded unconditionally and independently (one round trip), the segment's
+// parameters stay in registers while consecutive tiles share a segment, and
+// changes go to the tile's own slice of the change list.
+constexpr int kCountPer = 4;
+static_assert(SG_TILE % (SG_SIR_THREADS * kCountPer) == 0, "tile must be whole passes");
+
 template <int VARIANT, bool STATS, bool INPLACE>
 __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickArgs a)
 {
     __shared__ unsigned long long red[4][kWarps];
     __shared__ int32_t nch;
     const int tid = threadIdx.x, lane = tid & 31;
+    int32_t cur_seg = -1;
+    int64_t tick = 0, end_tick = 0;
+    uint32_t c0b = 0, key = 0, kinf = 0, krec = 0;
+    int32_t cs = 0, ci = 0, cr = 0, par = 0, lid_base = 0;
+    const uint32_t *lids = nullptr;
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
         const SgTile tile = a.tiles[t];
-        const SgSeg &sg = a.segs[tile.seg];
-        const int64_t tick = sg.tick0 + a.r;
-        if (tick >= sg.end_tick) {
+        if (tile.seg != cur_seg) {
+            const SgSeg &sg = a.segs[tile.seg];
+            cur_seg = tile.seg;
+            tick = sg.tick0 + a.r;
+            end_tick = sg.end_tick;
+            c0b = sg_c0base(tick);
+            key = sg.key;
+            kinf = sg.kinf;
+            krec = sg.krec;
+            cs = sg.cs;
+            ci = sg.ci;
+            cr = sg.cr;
+            par = INPLACE ? 0 : ((sg.par0 + a.r) & 1);
+            lids = sg.lids;
+            lid_base = sg.lid_base;
+        }
+        if (tick >= end_tick) {
             if (tid == 0) a.tile_nch[t] = 0;
             continue;
         }
-        const int par = INPLACE ? 0 : ((sg.par0 + a.r) & 1);
         const int32_t *sin = (const int32_t *)(par ? a.buf1 : a.buf0);
         int32_t *sout = (int32_t *)(INPLACE ? a.buf0 : (par ? a.buf0 : a.buf1));
-        const uint32_t c0b = sg_c0base(tick);
-        const uint32_t key = sg.key, kinf = sg.kinf, krec = sg.krec;
-        const int32_t cs = sg.cs, ci = sg.ci, cr = sg.cr;
         int32_t *tchanges = a.changes + tile.begin;
         unsigned long long nS = 0, nI = 0, nR = 0, eS = 0;
         if (tid == 0) nch = 0;
         __syncthreads();
-        // all loads of the thread's agents are issued before any is used
-        int32_t s[kPerThread], k[kPerThread];
-        uint32_t lid[kPerThread];
+        for (int32_t pass = tile.begin; pass < tile.end; pass += SG_SIR_THREADS * kCountPer) {
+            int32_t s[kCountPer], k[kCountPer];
+            uint32_t lid[kCountPer];
 #pragma unroll
-        for (int q = 0; q < kPerThread; ++q) {
-            const int32_t i = tile.begin + q * SG_SIR_THREADS + tid;
-            s[q] = i < tile.end ? sin[i] : INT32_MIN;
-        }
+            for (int q = 0; q < kCountPer; ++q) {
+                const int32_t i = pass + q * SG_SIR_THREADS + tid;
+                const bool v = i < tile.end;
+                s[q] = v ? sin[i] : INT32_MIN;
+                k[q] = v ? a.cnt[i] : 0;
+                lid[q] = lids ? (v ? __ldg(lids + i) : 0u) : (uint32_t)(i - lid_base);
+            }
 #pragma unroll
-        for (int q = 0; q < kPerThread; ++q) {
-            const int32_t i = tile.begin + q * SG_SIR_THREADS + tid;
-            k[q] = s[q] == cs ? a.cnt[i] : 0;
-        }
-#pragma unroll
-        for (int q = 0; q < kPerThread; ++q) {
-            const int32_t i = tile.begin + q * SG_SIR_THREADS + tid;
-            lid[q] = (s[q] == ci || k[q] > 0) ? seg_lid(sg, i) : 0u;
-        }
-#pragma unroll
-        for (int q = 0; q < kPerThread; ++q) {
-            const int32_t i = tile.begin + q * SG_SIR_THREADS + tid;
-            int32_t out = s[q];
-            bool has = false;
-            int32_t code = 0;
-            if (s[q] == ci) {
-                if (sg_philox_k23(c0b + 1u, lid[q], key) < krec) {
-                    out = cr;
-                    has = true;
-                    code = ~i;
-                }
-            } else if (k[q] > 0) {
-                bool inf = false;
-                if (VARIANT == 1) {
-                    inf = sg_philox_k23(c0b + 1u, lid[q], key) < kinf;
-                } else {
-                    for (int32_t j = 0; j < k[q]; ++j) {
-                        if (sg_philox_k23(c0b + 2u + (uint32_t)j, lid[q], key) < kinf) {
-                            inf = true;
-                            break;
-                        }
+            for (int q = 0; q < kCountPer; ++q) {
+                const int32_t i = pass + q * SG_SIR_THREADS + tid;
+                int32_t out = s[q];
+                bool has = false;
+                int32_t code = 0;
+                if (s[q] == ci) {
+                    if (sg_philox_k23(c0b + 1u, lid[q], key) < krec) {
+                        out = cr;
+                        has = true;
+                        code = ~i;
+                    }
+                } else if (s[q] == cs && k[q] > 0) {
+                    bool inf = false;
+                    if (VARIANT == 1) {
+                        inf = sg_philox_k23(c0b + 1u, lid[q], key) < kinf;
+                    } else {
+                        for (int32_t j = 0; j < k[q]; ++j)
+                            if (sg_philox_k23(c0b + 2u + (uint32_t)j, lid[q], key) < kinf) {
+                                inf = true;
+                                break;
+                            }
+                    }
+                    if (inf) {
+                        out = ci;
+                        has = true;
+                        code = i;
                     }
                 }
-                if (inf) {
-                    out = ci;
-                    has = true;
-                    code = i;
+                if (i < tile.end) {
+                    if (!INPLACE || has) sout[i] = out;
+                    if (STATS) {
+                        if (s[q] == cs) eS += (unsigned long long)(__ldg(a.off + i + 1) - __ldg(a.off + i));
+                        nS += (out == cs);
+                        nI += (out == ci);
+                        nR += (out == cr);
+                    }
                 }
-            }
-            if (i < tile.end) {
-                if (!INPLACE || has) sout[i] = out;
-                if (STATS) {
-                    if (s[q] == cs) eS += (unsigned long long)(__ldg(a.off + i + 1) - __ldg(a.off + i));
-                    nS += (out == cs);
-                    nI += (out == ci);
-                    nR += (out == cr);
+                const unsigned m = __ballot_sync(FULL_MASK, has);
+                if (m) {
+                    const int leader = __ffs(m) - 1;
+                    int32_t pos = 0;
+                    if (lane == leader) pos = atomicAdd(&nch, __popc(m));
+                    pos = __shfl_sync(FULL_MASK, pos, leader);
+                    if (has) tchanges[pos + __popc(m & ((1u << lane) - 1u))] = code;
                 }
-            }
-            const unsigned m = __ballot_sync(FULL_MASK, has);
-            if (m) {
-                const int leader = __ffs(m) - 1;
-                int32_t pos = 0;
-                if (lane == leader) pos = atomicAdd(&nch, __popc(m));
-                pos = __shfl_sync(FULL_MASK, pos, leader);
-                if (has) tchanges[pos + __popc(m & ((1u << lane) - 1u))] = code;
             }
         }
         __syncthreads();
         if (tid == 0) a.tile_nch[t] = nch;
-        if (STATS && sg.stats) block_flush4(nS, nI, nR, eS, sg.stats + 4 * (int64_t)a.r, red);
-        __syncthreads(); // nch is reset for the next tile only after every read
+        if (STATS && a.segs[tile.seg].stats)
+            block_flush4(nS, nI, nR, eS, a.segs[tile.seg].stats + 4 * (int64_t)a.r, red);
     }
 }
 
