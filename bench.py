@@ -373,13 +373,57 @@ def profile_case(args):
         eng.set_seed(SEED)
         prop = eng.add_property("state", np.int32, init=st0)
         eng.add_sir(prop, BETA, GAMMA, variant="B", strategy=args.strategy, codes=CODES)
-        stats, _ = eng.run(0, TICKS, stats=True)
+        if args.flavour >= 0:
+            eng.set_tune(blocks_per_sm=args.bps, count_flavour=args.flavour)
+        stats, _ = eng.run(0, TICKS, stats=args.profile_stats)
         active = eng.last_run_active(TICKS)
         final = eng.get_property(prop)
     print("profile case done: %d agents, %d ticks, %d infected or recovered at the end"
           % (args.agents, TICKS, int((final != CODES[0]).sum())))
-    for t in (0, 5, 10, 15, 20, 25, 30, 40, 60, 100, 150, 199):
-        print("tick %3d  S %9d  I %9d  R %9d  E_S %10d  processed %9d" % ((t,) + tuple(stats[t]) + (active[t],)))
+    if args.profile_stats:
+        for t in (0, 5, 10, 15, 20, 25, 30, 40, 60, 100, 150, 199):
+            print("tick %3d  S %9d  I %9d  R %9d  E_S %10d  processed %9d" % ((t,) + tuple(stats[t]) + (active[t],)))
+
+
+def sweep(args):
+    """Device time of simulate(200) for every count-step launch configuration."""
+    import torch
+
+    from sagesim_gb300 import Engine
+
+    off, idx, st0, lids = build_workload(args.agents)
+    stream = torch.cuda.Stream()
+    rows = []
+    with torch.cuda.stream(stream):
+        eng = Engine(stream=stream.cuda_stream)
+        eng.set_graph(off, idx, symmetric=True)
+        eng.set_logical_ids(lids)
+        eng.set_seed(SEED)
+        prop = eng.add_property("state", np.int32, init=st0)
+        eng.add_sir(prop, BETA, GAMMA, variant="B", strategy="count", codes=CODES)
+        eng.snapshot()
+        ref = None
+        for bps in (4, 8, 16):
+            for fl in range(8):
+                eng.set_tune(blocks_per_sm=bps, count_flavour=fl)
+                for _ in range(2):
+                    eng.restore()
+                    eng.run_async(0, TICKS)
+                stream.synchronize()
+                ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                ev0.record(stream)
+                for _ in range(5):
+                    eng.restore()
+                    eng.run_async(0, TICKS)
+                ev1.record(stream)
+                stream.synchronize()
+                fin = eng.get_property(prop)
+                ref = fin if ref is None else ref
+                rows.append({"blocks_per_sm": bps, "count_flavour": fl, "ms_per_step": ev0.elapsed_time(ev1) / 5,
+                             "same_result": bool(np.array_equal(fin, ref))})
+        eng.close()
+    for r in sorted(rows, key=lambda r: r["ms_per_step"]):
+        print(json.dumps(r))
 
 
 def main():
@@ -390,6 +434,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--strategy", default="count", choices=["count", "frontier", "pull"])
     ap.add_argument("--agents", type=int, default=N_AGENTS)
+    ap.add_argument("--profile-stats", action="store_true",
+                    help="with --profile-case: collect and print per-tick S/I/R/E_S")
+    ap.add_argument("--flavour", type=int, default=-1, help="count-step flavour for --profile-case")
+    ap.add_argument("--bps", type=int, default=8, help="blocks per SM for --profile-case")
+    ap.add_argument("--sweep", action="store_true",
+                    help="time every count-step flavour x blocks/SM on the workload and exit")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the ensemble and serving sections")
     ap.add_argument("--profile-case", action="store_true",
@@ -400,6 +450,9 @@ def main():
         return
     if args.profile_case:
         profile_case(args)
+        return
+    if args.sweep:
+        sweep(args)
         return
 
     import torch

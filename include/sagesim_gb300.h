@@ -122,6 +122,18 @@ typedef struct sg_stats {
     double device_ms;       /* device time of the run (CUDA events)             */
 } sg_stats;
 
+/* Launch configuration the autotuner chooses between (all give identical results). */
+typedef struct sg_tune {
+    int32_t strategy;          /* SG_SIR_PULL or SG_SIR_COUNT                     */
+    int32_t blocks_per_sm;     /* persistent grid = blocks_per_sm x SM count     */
+    int32_t thread_row;        /* rows up to this length: one lane; longer: warp */
+    int32_t mega_row;          /* rows longer than this: a whole block           */
+    int32_t count_flavour;     /* count step: 1 = 8 agents per thread (else 4),  */
+                               /* 2 = warp-dense SIR-B draws, 4 = count and RNG  */
+                               /* key loaded only where needed                   */
+    double us_per_tick;        /* measured by sg_batch_tune (output)             */
+} sg_tune;
+
 /* ---- engine lifecycle ------------------------------------------------------- */
 int sg_engine_create(const sg_engine_cfg *cfg, sg_engine **out);
 int sg_engine_destroy(sg_engine *e);
@@ -177,6 +189,10 @@ int sg_run(sg_engine *e, int64_t tick0, int32_t nticks, int64_t *tick_stats, sg_
 int sg_run_async(sg_engine *e, int64_t tick0, int32_t nticks, int32_t use_graph);
 int sg_synchronize(sg_engine *e);
 
+/* Launch configuration of the engine's SIR kernels (strategy is ignored: it is
+ * a property of the step). All configurations give identical results. */
+int sg_engine_set_tune(sg_engine *e, const sg_tune *t);
+
 /* Agents the SIR step processed in each tick of the last sg_run/sg_run_async
  * (the active list length for the frontier strategy, the step's agent range
  * otherwise); n = number of ticks to report. Synchronizes the stream. */
@@ -218,14 +234,6 @@ typedef struct sg_scenario_desc {
     int32_t flags;             /* SG_GRAPH_SYMMETRIC when the CSR is its own transpose     */
 } sg_scenario_desc;
 
-/* Launch configuration the autotuner chooses between (all give identical results). */
-typedef struct sg_tune {
-    int32_t strategy;          /* SG_SIR_PULL or SG_SIR_COUNT                     */
-    int32_t blocks_per_sm;     /* persistent grid = blocks_per_sm x SM count     */
-    int32_t thread_row;        /* rows up to this length: one lane; longer: warp */
-    int32_t mega_row;          /* rows longer than this: a whole block           */
-    double us_per_tick;        /* measured by sg_batch_tune (output)             */
-} sg_tune;
 
 int sg_batch_create(const sg_engine_cfg *cfg, sg_batch **out);
 int sg_batch_destroy(sg_batch *b);

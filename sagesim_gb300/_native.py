@@ -84,7 +84,7 @@ class ScenarioDesc(ctypes.Structure):
 class Tune(ctypes.Structure):
     _fields_ = [("strategy", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
                 ("thread_row", ctypes.c_int32), ("mega_row", ctypes.c_int32),
-                ("us_per_tick", ctypes.c_double)]
+                ("count_flavour", ctypes.c_int32), ("us_per_tick", ctypes.c_double)]
 
 
 class ServerCfg(ctypes.Structure):
@@ -122,6 +122,7 @@ SIGNATURES = {
     "sg_run_async": [_P, _I64, _I32, _I32],
     "sg_synchronize": [_P],
     "sg_last_run_active": [_P, _P, _I32],
+    "sg_engine_set_tune": [_P, ctypes.POINTER(Tune)],
     "sg_snapshot": [_P],
     "sg_restore": [_P],
     "sg_profile_enable": [_P, _I32],

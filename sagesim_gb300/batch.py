@@ -75,8 +75,8 @@ class Batch:
     def commit(self):
         self._ck(self._lib.sg_batch_commit(self._h))
 
-    def set_tune(self, strategy="count", blocks_per_sm=8, thread_row=32, mega_row=2048):
-        t = N.Tune(STRATEGIES[strategy], blocks_per_sm, thread_row, mega_row, 0.0)
+    def set_tune(self, strategy="count", blocks_per_sm=8, thread_row=32, mega_row=2048, count_flavour=0):
+        t = N.Tune(STRATEGIES[strategy], blocks_per_sm, thread_row, mega_row, count_flavour, 0.0)
         self._ck(self._lib.sg_batch_set_tune(self._h, ctypes.byref(t)))
 
     def get_tune(self):
@@ -120,4 +120,4 @@ class Batch:
 def _tune_dict(t):
     inv = {v: k for k, v in STRATEGIES.items()}
     return {"strategy": inv[t.strategy], "blocks_per_sm": t.blocks_per_sm, "thread_row": t.thread_row,
-            "mega_row": t.mega_row, "us_per_tick": t.us_per_tick}
+            "mega_row": t.mega_row, "count_flavour": t.count_flavour, "us_per_tick": t.us_per_tick}

@@ -121,6 +121,8 @@ int SgPool::allocate(int64_t acap, int64_t ecap, int64_t max_scen, bool transpos
     POOL_CK(cnt.reserve((size_t)std::max<int64_t>(acap, 1) * 4));
     POOL_CK(changes.reserve((size_t)std::max<int64_t>(acap, 1) * 4));
     POOL_CK(tile_nch.reserve((size_t)tile_cap * 4));
+    POOL_CK(chunks.reserve(((size_t)acap / 32 + (size_t)tile_cap + 1) * sizeof(SgChunk)));
+    POOL_CK(rowsegs.reserve(((size_t)ecap / 128 + 64) * sizeof(SgRowSeg)));
     POOL_CK(tiles.reserve((size_t)tile_cap * sizeof(SgTile)));
     POOL_CK(segs.reserve((size_t)seg_cap * sizeof(SgSeg)));
     any_lids = with_lids;
@@ -132,7 +134,7 @@ int SgPool::allocate(int64_t acap, int64_t ecap, int64_t max_scen, bool transpos
 
 bool SgPool::fits(int64_t n, int64_t nnz) const
 {
-    return agents.largest() >= n + 1 && (nnz == 0 || edges.largest() >= nnz) &&
+    return agents.largest() >= ((n + 1 + 3) & ~int64_t(3)) && (nnz == 0 || edges.largest() >= nnz) &&
            (int64_t)scen.size() < seg_cap;
 }
 
@@ -146,11 +148,14 @@ int SgPool::place(const sg_scenario_desc &d, const int32_t *loff, const int32_t 
     if (!sym && all_symmetric) return fail(SG_ERR_INVALID, "pool holds symmetric graphs only");
     if (llids && !any_lids) return fail(SG_ERR_INVALID, "pool was allocated without logical ids");
     if ((int64_t)scen.size() >= seg_cap) return fail(SG_ERR_BUDGET, "scenario table full");
-    const int64_t ab = agents.take(n + 1);
+    // agent slots in multiples of 4 keep every scenario's first agent 16-byte
+    // aligned (128-bit state loads)
+    const int64_t aslots = (n + 1 + 3) & ~int64_t(3);
+    const int64_t ab = agents.take(aslots);
     if (ab < 0) return fail(SG_ERR_BUDGET, "no room for the scenario's agents");
     const int64_t eb = nnz > 0 ? edges.take(nnz) : 0;
     if (eb < 0) {
-        agents.give(ab, n + 1);
+        agents.give(ab, aslots);
         return fail(SG_ERR_BUDGET, "no room for the scenario's edges");
     }
     POOL_CK(cudaSetDevice(device));
@@ -213,7 +218,7 @@ void SgPool::release(int32_t sid)
     auto it = sid_slot.find(sid);
     if (it == sid_slot.end()) return;
     const size_t slot = it->second;
-    agents.give(scen[slot].agent_base, scen[slot].n + 1);
+    agents.give(scen[slot].agent_base, (scen[slot].n + 1 + 3) & ~int64_t(3));
     if (scen[slot].nnz) edges.give(scen[slot].edge_base, scen[slot].nnz);
     s_long_rows_.erase(sid);
     scen.erase(scen.begin() + (ptrdiff_t)slot);
@@ -296,6 +301,7 @@ int SgPool::enqueue(int32_t nticks, bool capturing)
     a.tiles = tiles.as<SgTile>();
     a.ntiles = (int32_t)htiles.size();
     a.thread_row = tune.thread_row;
+    a.flavour = tune.count_flavour;
     a.mega = mega.as<SgMega>();
     a.nmega = (int32_t)hmega.size();
     a.mega_blocks = std::min<int32_t>(a.nmega, sm_count);
@@ -303,11 +309,19 @@ int SgPool::enqueue(int32_t nticks, bool capturing)
     a.cnt = cnt.as<int32_t>();
     a.changes = changes.as<int32_t>();
     a.tile_nch = tile_nch.as<int32_t>();
+    a.chunks = chunks.as<SgChunk>();
+    a.nchunks = nchunks.as<int32_t>();
+    a.rowsegs = rowsegs.as<SgRowSeg>();
+    a.nrowsegs = nrowsegs.as<int32_t>();
     a.toff = all_symmetric ? off.as<int32_t>() : toff.as<int32_t>();
     a.tidx = all_symmetric ? idx.as<int32_t>() : tidx.as<int32_t>();
     const int grid = std::max(1, std::min<int>(a.ntiles, sm_count * std::max(tune.blocks_per_sm, 1)));
     const int variant = builtin == SG_BUILTIN_SIR_A ? 1 : 2;
     if (a.ntiles == 0) return SG_OK;
+    if (count) {
+        POOL_CK(cudaMemsetAsync(nchunks.p, 0, (size_t)nticks * 4, stream));
+        POOL_CK(cudaMemsetAsync(nrowsegs.p, 0, (size_t)nticks * 4, stream));
+    }
     for (int32_t r = 0; r < nticks; ++r) {
         a.r = r;
         cudaError_t ce;
@@ -331,6 +345,11 @@ int SgPool::run(int32_t nticks, bool use_graph)
         if (rc) return rc;
     }
     const bool count = tune.strategy == SG_SIR_COUNT;
+    if (count && nticks > nchunks_cap) { // before any capture: no allocation inside a graph
+        POOL_CK(nchunks.reserve((size_t)nticks * 4));
+        POOL_CK(nrowsegs.reserve((size_t)nticks * 4));
+        nchunks_cap = nticks;
+    }
     if (count) {
         int rc = consolidate();
         if (rc) return rc;
@@ -560,7 +579,7 @@ int sg_batch_commit(sg_batch *b)
     int64_t agents = 0, nnz = 0;
     bool transpose = false, lids = false;
     for (auto &s : b->staged) {
-        agents += s.d.n_agents + 1;
+        agents += (s.d.n_agents + 1 + 3) & ~int64_t(3);
         nnz += s.d.nnz;
         transpose |= !(s.d.flags & SG_GRAPH_SYMMETRIC);
         lids |= !s.lids.empty();
@@ -583,7 +602,8 @@ int sg_batch_set_tune(sg_batch *b, const sg_tune *t)
 {
     if (!b || !t) return SG_ERR_INVALID;
     if (t->strategy != SG_SIR_PULL && t->strategy != SG_SIR_COUNT) return b->pool.fail(SG_ERR_INVALID, "bad strategy");
-    if (t->blocks_per_sm < 1 || t->blocks_per_sm > 32 || t->thread_row < 1 || t->mega_row < kLongRowFloor)
+    if (t->blocks_per_sm < 1 || t->blocks_per_sm > 32 || t->thread_row < 1 || t->mega_row < kLongRowFloor ||
+        t->count_flavour < 0 || t->count_flavour > 7)
         return b->pool.fail(SG_ERR_INVALID, "tune parameters out of range");
     const bool mega_changed = t->mega_row != b->pool.tune.mega_row;
     b->pool.tune = *t;
@@ -667,26 +687,30 @@ int sg_batch_tune(sg_batch *b, int32_t ticks, sg_tune *best)
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (int32_t strategy : {SG_SIR_COUNT, SG_SIR_PULL})
-        for (int32_t bps : {2, 4, 8, 16})
-            for (int32_t trow : {16, 32, 64})
-                for (int32_t mrow : {1024, 4096}) {
-                    sg_tune t{strategy, bps, trow, mrow, 0.0};
-                    if ((rc = sg_batch_set_tune(b, &t)) != SG_OK) break;
-                    if ((rc = p.restore()) != SG_OK) break;
-                    // untimed pass: count init, table rebuild, caches
-                    if ((rc = p.run(1, false)) != SG_OK) break;
-                    if ((rc = p.restore()) != SG_OK) break;
-                    if (strategy == SG_SIR_COUNT && (rc = p.run(0, false)) != SG_OK) break;
-                    cudaEventRecord(e0, p.stream);
-                    if ((rc = p.run(ticks, false)) != SG_OK) break;
-                    cudaEventRecord(e1, p.stream);
-                    cudaEventSynchronize(e1);
-                    float ms = 0.f;
-                    cudaEventElapsedTime(&ms, e0, e1);
-                    t.us_per_tick = 1e3 * ms / ticks;
-                    if (t.us_per_tick < win.us_per_tick) win = t;
-                }
+    // pull: blocks/SM x lane/warp row split x block-row threshold; count:
+    // blocks/SM x count-step flavour (its rows matter only once per run)
+    std::vector<sg_tune> cands;
+    for (int32_t bps : {2, 4, 8, 16}) {
+        for (int32_t trow : {16, 32, 64})
+            for (int32_t mrow : {1024, 4096}) cands.push_back(sg_tune{SG_SIR_PULL, bps, trow, mrow, 0, 0.0});
+        for (int32_t fl = 0; fl < 8; ++fl) cands.push_back(sg_tune{SG_SIR_COUNT, bps, 32, 2048, fl, 0.0});
+    }
+    for (sg_tune t : cands) {
+        if ((rc = sg_batch_set_tune(b, &t)) != SG_OK) break;
+        if ((rc = p.restore()) != SG_OK) break;
+        // untimed pass: count init, table rebuild, caches
+        if ((rc = p.run(1, false)) != SG_OK) break;
+        if ((rc = p.restore()) != SG_OK) break;
+        if (t.strategy == SG_SIR_COUNT && (rc = p.run(0, false)) != SG_OK) break;
+        cudaEventRecord(e0, p.stream);
+        if ((rc = p.run(ticks, false)) != SG_OK) break;
+        cudaEventRecord(e1, p.stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        t.us_per_tick = 1e3 * ms / ticks;
+        if (t.us_per_tick < win.us_per_tick) win = t;
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     int rc2 = sg_batch_set_tune(b, rc == SG_OK ? &win : &orig);

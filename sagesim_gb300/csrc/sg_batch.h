@@ -56,7 +56,9 @@ struct SgPool {
 
     int64_t agent_cap = 0, edge_cap = 0;
     SgRanges agents, edges;
-    SgDev off, idx, toff, tidx, st[2], cnt, changes, tile_nch, lids, segs, tiles, mega;
+    SgDev off, idx, toff, tidx, st[2], cnt, changes, tile_nch, lids, segs, tiles, mega, chunks, nchunks,
+        rowsegs, nrowsegs;
+    int32_t nchunks_cap = 0;
     SgDev snap_st[2], snap_cnt;
     bool any_lids = false, all_symmetric = true;
     int64_t seg_cap = 0, tile_cap = 0, mega_cap = 0;
@@ -72,7 +74,7 @@ struct SgPool {
     bool tables_dirty = true;
     uint64_t version = 1;
 
-    sg_tune tune{SG_SIR_COUNT, 8, 32, 2048, 0.0};
+    sg_tune tune{SG_SIR_COUNT, 16, 32, 2048, 0, 0.0};
     cudaGraphExec_t graph = nullptr;
     int32_t graph_nticks = -1;
     uint64_t graph_version = 0;

@@ -74,13 +74,14 @@ struct sg_engine {
     int32_t next_step_id = 0;
 
     // scratch of the count strategy and of per-tick statistics
-    SgDev cnt, changes, tile_nch, stats;
+    SgDev cnt, changes, tile_nch, stats, chunks, nchunks, rowsegs, nrowsegs;
     SgDev flist[2], flen, fnch, fmark, fstats_init, fstats_delta; // frontier strategy
     SgDev transpose_tmp, scan_tmp;
     SgDev prop_table; // sg_prop_dev per property, for compiled steps
 
     SgProfiler prof;
     int hub_deg = 32;
+    sg_tune tune{SG_SIR_COUNT, 16, 32, 2048, 0, 0.0};
     int32_t last_nticks = 0;
 
     // CUDA graph of the tick loop (sg_run_async with use_graph)
@@ -559,7 +560,8 @@ static SgTickArgs base_args(sg_engine *e, SgStep *s, int32_t r, bool inplace)
     a.tiles = s->tiles.as<SgTile>();
     a.ntiles = s->ntiles;
     a.r = r;
-    a.thread_row = e->hub_deg;
+    a.thread_row = e->tune.thread_row;
+    a.flavour = e->tune.count_flavour;
     a.mega = s->mega.as<SgMega>();
     a.nmega = s->nmega;
     a.mega_blocks = std::min(s->nmega, e->sm_count);
@@ -567,6 +569,10 @@ static SgTickArgs base_args(sg_engine *e, SgStep *s, int32_t r, bool inplace)
     a.cnt = e->cnt.as<int32_t>();
     a.changes = e->changes.as<int32_t>();
     a.tile_nch = e->tile_nch.as<int32_t>();
+    a.chunks = e->chunks.as<SgChunk>();
+    a.nchunks = e->nchunks.as<int32_t>();
+    a.rowsegs = e->rowsegs.as<SgRowSeg>();
+    a.nrowsegs = e->nrowsegs.as<int32_t>();
     const bool sym = (e->graph_flags & SG_GRAPH_SYMMETRIC) != 0;
     a.toff = sym ? e->off.as<int32_t>() : e->toff.as<int32_t>();
     a.tidx = sym ? e->idx.as<int32_t>() : e->tidx.as<int32_t>();
@@ -583,7 +589,7 @@ static SgTickArgs base_args(sg_engine *e, SgStep *s, int32_t r, bool inplace)
 
 static int grid_for(sg_engine *e, int32_t ntiles)
 {
-    const int cap = e->sm_count * 8;
+    const int cap = e->sm_count * std::max(e->tune.blocks_per_sm, 1);
     return std::max(1, std::min(ntiles, cap));
 }
 
@@ -626,6 +632,8 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
     if (pl.count_step) {
         SgStep *s = pl.count_step;
         SgTickArgs a = base_args(e, s, 0, pl.count_inplace);
+        SG_CK(cudaMemsetAsync(e->nchunks.p, 0, (size_t)std::max(nticks, 1) * 4, e->stream));
+        SG_CK(cudaMemsetAsync(e->nrowsegs.p, 0, (size_t)std::max(nticks, 1) * 4, e->stream));
         SG_PROF_LAUNCH("sir_count_init",
                        sg_launch_sir_count_init(a, grid_for(e, s->ntiles) + a.mega_blocks, e->stream));
     }
@@ -728,8 +736,13 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
         rc = prepare_step(e, s, tick0, stats);
         if (rc) return rc;
     }
-    if (pl.count_step)
+    if (pl.count_step) {
         SG_CK(e->tile_nch.reserve((size_t)std::max(pl.count_step->ntiles, 1) * 4));
+        SG_CK(e->chunks.reserve(((size_t)e->n / 32 + pl.count_step->ntiles + 1) * sizeof(SgChunk)));
+        SG_CK(e->nchunks.reserve((size_t)std::max(nticks, 1) * 4));
+        SG_CK(e->rowsegs.reserve(((size_t)e->nnz / 128 + 64) * sizeof(SgRowSeg)));
+        SG_CK(e->nrowsegs.reserve((size_t)std::max(nticks, 1) * 4));
+    }
     return SG_OK;
 }
 
@@ -849,6 +862,17 @@ int sg_run_async(sg_engine *e, int64_t tick0, int32_t nticks, int32_t use_graph)
     }
     SG_CK(cudaGraphLaunch(e->graph_exec, e->stream));
     finish_run(e, pl, nticks);
+    return SG_OK;
+}
+
+int sg_engine_set_tune(sg_engine *e, const sg_tune *t)
+{
+    if (!e || !t) return SG_ERR_INVALID;
+    if (t->blocks_per_sm < 1 || t->blocks_per_sm > 32 || t->thread_row < 1 || t->count_flavour < 0 ||
+        t->count_flavour > 7)
+        return e->fail(SG_ERR_INVALID, "tune parameters out of range");
+    e->tune = *t;
+    e->version++;
     return SG_OK;
 }
 

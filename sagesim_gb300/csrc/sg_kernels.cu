@@ -437,26 +437,126 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_init_kernel(SgTickAr
 
 constexpr int kPerThread = SG_TILE / SG_SIR_THREADS; // agents per thread in a tile
 
-// Count-strategy step. The tail of an epidemic makes this a streaming pass over
-// every agent, so the kernel is built for memory-level parallelism: each
-// thread handles kCountPer agents per pass with their state, count and RNG key
-// loaded unconditionally and independently (one round trip), the segment's
-// parameters stay in registers while consecutive tiles share a segment, and
-// changes go to the tile's own slice of the change list.
-constexpr int kCountPer = 4;
-static_assert(SG_TILE % (SG_SIR_THREADS * kCountPer) == 0, "tile must be whole passes");
+// Warp-dense SIR-B draws. Lane l holds up to kCountPer susceptible agents; agent
+// q needs draws j = 0 .. k[q]-1 (salt 2 + j) until one is below beta. The warp
+// lays out the first min(k, kWarpDenseCap) draws of all its agents in one
+// sequence (exclusive scan of the lanes' totals) and evaluates 32 of them per
+// step, one per lane: the owner of draw d is found by a shuffle binary search
+// over the lanes' scan values. Hits are flagged in shared memory. Agents with
+// more draws and no hit continue with 32-wide warp batches. Returns the bit
+// mask of the calling lane's infected agents. Every lane must call it.
+constexpr int32_t kWarpDenseCap = 32;
 
-template <int VARIANT, bool STATS, bool INPLACE>
+template <int P>
+__device__ __forceinline__ unsigned warp_dense_sirb(const int32_t (&k)[P], const uint32_t (&lid)[P],
+                                                    uint32_t c0b, uint32_t key, uint32_t kinf, int lane,
+                                                    unsigned char *flags /* 32 * P bytes of this warp */)
+{
+    int32_t c[P], tot = 0;
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+        c[q] = k[q] < kWarpDenseCap ? k[q] : kWarpDenseCap;
+        tot += c[q];
+        flags[lane * P + q] = 0;
+    }
+    int32_t x = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int32_t y = __shfl_up_sync(FULL_MASK, x, o);
+        if (lane >= o) x += y;
+    }
+    const int32_t base = x - tot;
+    const int32_t W = __shfl_sync(FULL_MASK, x, 31);
+    __syncwarp();
+    for (int32_t d0 = 0; d0 < W; d0 += 32) {
+        const int32_t d = d0 + lane;
+        int32_t lo = 0; // owner: the last lane with base <= d
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const int32_t b = __shfl_sync(FULL_MASK, base, (lo + step) & 31);
+            if (lo + step < 32 && b <= d) lo += step;
+        }
+        int32_t off = d - __shfl_sync(FULL_MASK, base, lo);
+        int32_t qsel = 0;
+        uint32_t l = 0;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            const int32_t cq = __shfl_sync(FULL_MASK, c[q], lo);
+            const uint32_t lq = __shfl_sync(FULL_MASK, lid[q], lo);
+            if (qsel == q) {
+                if (off < cq) {
+                    l = lq;
+                    qsel = q + 100; // found: stop advancing
+                } else {
+                    off -= cq;
+                    qsel = q + 1;
+                }
+            }
+        }
+        if (d < W && qsel >= 100 && sg_philox_k23(c0b + 2u + (uint32_t)off, l, key) < kinf)
+            flags[lo * P + (qsel - 100)] = 1;
+    }
+    __syncwarp();
+    unsigned bits = 0;
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+        bool inf = flags[lane * P + q] != 0;
+        unsigned m = __ballot_sync(FULL_MASK, !inf && k[q] > kWarpDenseCap);
+        while (m) {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            const int32_t bk = __shfl_sync(FULL_MASK, k[q], src);
+            const uint32_t bl = __shfl_sync(FULL_MASK, lid[q], src);
+            const bool h = warp_draws((uint32_t)kWarpDenseCap, bk - kWarpDenseCap, c0b, bl, key, kinf, lane);
+            if (lane == src) inf = h;
+        }
+        if (inf) bits |= 1u << q;
+    }
+    __syncwarp(); // flags are reused by the next call
+    return bits;
+}
+
+// A changed agent whose transpose row is longer than kSegRow is handed to the
+// scatter as row segments of kSegRow entries on their own work list, so no
+// single warp walks a hub's whole row; the chunk pass skips such rows.
+constexpr int32_t kSegRow = 256;
+
+__device__ __forceinline__ void publish_long_row(const SgTickArgs &a, int32_t g, int32_t delta)
+{
+    const int32_t b = __ldg(a.toff + g), e = __ldg(a.toff + g + 1);
+    if (e - b <= kSegRow) return;
+    const int32_t nseg = (e - b + kSegRow - 1) / kSegRow;
+    const int32_t base = atomicAdd(a.nrowsegs + a.r, nseg);
+    for (int32_t j = 0; j < nseg; ++j) {
+        const int32_t sb = b + j * kSegRow;
+        a.rowsegs[base + j] = SgRowSeg{sb, min(sb + kSegRow, e), delta, 0};
+    }
+}
+
+// Count-strategy step. Late in an epidemic this is a streaming pass over every
+// agent; at its peak most susceptible agents draw. Flavours (all give the
+// same result; the autotuner picks one):
+//   PER    4: one agent per thread per 256-agent stripe (scalar loads); 8: two
+//          runs of 4 consecutive agents per thread read with 128-bit loads
+//   DENSE  SIR-B draws laid out warp-densely (warp_dense_sirb) instead of per-lane loops
+//   LAZY   the count and RNG key are loaded only for agents that need them (a
+//          second round trip) instead of unconditionally with the state
+// The segment's parameters stay in registers while consecutive tiles share a
+// segment, and changes go to the tile's own slice of the change list.
+template <int VARIANT, bool STATS, bool INPLACE, int PER, bool DENSE, bool LAZY>
 __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickArgs a)
 {
+    static_assert(SG_TILE % (SG_SIR_THREADS * PER) == 0, "tile must be whole passes");
     __shared__ unsigned long long red[4][kWarps];
-    __shared__ int32_t nch;
+    __shared__ int32_t nch, chunk_base;
+    __shared__ unsigned char wflags[DENSE ? SG_SIR_THREADS * PER : 1];
     const int tid = threadIdx.x, lane = tid & 31;
     int32_t cur_seg = -1;
     int64_t tick = 0, end_tick = 0;
     uint32_t c0b = 0, key = 0, kinf = 0, krec = 0;
     int32_t cs = 0, ci = 0, cr = 0, par = 0, lid_base = 0;
     const uint32_t *lids = nullptr;
+    SgPhiloxKeys ks = sg_philox_keys(0);
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
         const SgTile tile = a.tiles[t];
         if (tile.seg != cur_seg) {
@@ -466,6 +566,7 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickAr
             end_tick = sg.end_tick;
             c0b = sg_c0base(tick);
             key = sg.key;
+            ks = sg_philox_keys(key);
             kinf = sg.kinf;
             krec = sg.krec;
             cs = sg.cs;
@@ -485,25 +586,94 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickAr
         unsigned long long nS = 0, nI = 0, nR = 0, eS = 0;
         if (tid == 0) nch = 0;
         __syncthreads();
-        for (int32_t pass = tile.begin; pass < tile.end; pass += SG_SIR_THREADS * kCountPer) {
-            int32_t s[kCountPer], k[kCountPer];
-            uint32_t lid[kCountPer];
+        for (int32_t pass = tile.begin; pass < tile.end; pass += SG_SIR_THREADS * PER) {
+            // agent of slot q: PER == 4 -> strided (pass + q*256 + tid, scalar
+            // coalesced loads); PER == 8 -> two runs of 4 consecutive agents per
+            // thread (pass + (q/4)*1024 + tid*4 + q%4) read with 128-bit loads
+            auto agent = [&](int q) -> int32_t {
+                return PER == 8 ? pass + (q >> 2) * (SG_SIR_THREADS * 4) + tid * 4 + (q & 3)
+                                : pass + q * SG_SIR_THREADS + tid;
+            };
+            int32_t s[PER], k[PER];
+            uint32_t lid[PER];
+            if (PER == 8) {
 #pragma unroll
-            for (int q = 0; q < kCountPer; ++q) {
-                const int32_t i = pass + q * SG_SIR_THREADS + tid;
-                const bool v = i < tile.end;
-                s[q] = v ? sin[i] : INT32_MIN;
-                k[q] = v ? a.cnt[i] : 0;
-                lid[q] = lids ? (v ? __ldg(lids + i) : 0u) : (uint32_t)(i - lid_base);
+                for (int g = 0; g < 2; ++g) {
+                    const int32_t b = agent(g * 4);
+                    if (b + 3 < tile.end && (b & 3) == 0) {
+                        const int4 v = *reinterpret_cast<const int4 *>(sin + b);
+                        s[g * 4] = v.x;
+                        s[g * 4 + 1] = v.y;
+                        s[g * 4 + 2] = v.z;
+                        s[g * 4 + 3] = v.w;
+                        if (!LAZY) {
+                            const int4 c = *reinterpret_cast<const int4 *>(a.cnt + b);
+                            k[g * 4] = c.x;
+                            k[g * 4 + 1] = c.y;
+                            k[g * 4 + 2] = c.z;
+                            k[g * 4 + 3] = c.w;
+                            if (lids) {
+                                const uint4 l = __ldg(reinterpret_cast<const uint4 *>(lids + b));
+                                lid[g * 4] = l.x;
+                                lid[g * 4 + 1] = l.y;
+                                lid[g * 4 + 2] = l.z;
+                                lid[g * 4 + 3] = l.w;
+                            } else {
+#pragma unroll
+                                for (int e = 0; e < 4; ++e) lid[g * 4 + e] = (uint32_t)(b + e - lid_base);
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            const int32_t i = b + e;
+                            const bool v = i < tile.end;
+                            s[g * 4 + e] = v ? sin[i] : INT32_MIN;
+                            if (!LAZY) {
+                                k[g * 4 + e] = v ? a.cnt[i] : 0;
+                                lid[g * 4 + e] = lids ? (v ? __ldg(lids + i) : 0u) : (uint32_t)(i - lid_base);
+                            }
+                        }
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < PER; ++q) {
+                    const int32_t i = agent(q);
+                    const bool v = i < tile.end;
+                    s[q] = v ? sin[i] : INT32_MIN;
+                    if (!LAZY) {
+                        k[q] = v ? a.cnt[i] : 0;
+                        lid[q] = lids ? (v ? __ldg(lids + i) : 0u) : (uint32_t)(i - lid_base);
+                    }
+                }
+            }
+            if (LAZY) {
+#pragma unroll
+                for (int q = 0; q < PER; ++q) k[q] = s[q] == cs ? a.cnt[agent(q)] : 0;
+#pragma unroll
+                for (int q = 0; q < PER; ++q) {
+                    const int32_t i = agent(q);
+                    lid[q] = (s[q] == ci || (s[q] == cs && k[q] > 0))
+                                 ? (lids ? __ldg(lids + i) : (uint32_t)(i - lid_base))
+                                 : 0u;
+                }
+            }
+            unsigned inf_bits = 0;
+            if (VARIANT == 2 && DENSE) {
+                int32_t kd[PER];
+#pragma unroll
+                for (int q = 0; q < PER; ++q) kd[q] = s[q] == cs ? k[q] : 0;
+                inf_bits = warp_dense_sirb<PER>(kd, lid, c0b, key, kinf, lane, wflags + (tid >> 5) * 32 * PER);
             }
 #pragma unroll
-            for (int q = 0; q < kCountPer; ++q) {
-                const int32_t i = pass + q * SG_SIR_THREADS + tid;
+            for (int q = 0; q < PER; ++q) {
+                const int32_t i = agent(q);
                 int32_t out = s[q];
                 bool has = false;
                 int32_t code = 0;
                 if (s[q] == ci) {
-                    if (sg_philox_k23(c0b + 1u, lid[q], key) < krec) {
+                    if (sg_philox_k23_keys(c0b + 1u, lid[q], ks) < krec) {
                         out = cr;
                         has = true;
                         code = ~i;
@@ -511,10 +681,12 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickAr
                 } else if (s[q] == cs && k[q] > 0) {
                     bool inf = false;
                     if (VARIANT == 1) {
-                        inf = sg_philox_k23(c0b + 1u, lid[q], key) < kinf;
+                        inf = sg_philox_k23_keys(c0b + 1u, lid[q], ks) < kinf;
+                    } else if (DENSE) {
+                        inf = ((inf_bits >> q) & 1u) != 0;
                     } else {
                         for (int32_t j = 0; j < k[q]; ++j)
-                            if (sg_philox_k23(c0b + 2u + (uint32_t)j, lid[q], key) < kinf) {
+                            if (sg_philox_k23_keys(c0b + 2u + (uint32_t)j, lid[q], ks) < kinf) {
                                 inf = true;
                                 break;
                             }
@@ -542,17 +714,92 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickAr
                     pos = __shfl_sync(FULL_MASK, pos, leader);
                     if (has) tchanges[pos + __popc(m & ((1u << lane) - 1u))] = code;
                 }
+                if (has && a.rowsegs) publish_long_row(a, i, code >= 0 ? 1 : -1);
             }
         }
         __syncthreads();
-        if (tid == 0) a.tile_nch[t] = nch;
+        {
+            // publish the tile's change count and its 32-change chunks to the
+            // scatter's work list (one atomic per tile with changes)
+            const int32_t n = nch;
+            const int32_t c = (n + 31) >> 5;
+            if (tid == 0) {
+                a.tile_nch[t] = n;
+                if (a.chunks && n > 0) chunk_base = atomicAdd(a.nchunks + a.r, c);
+            }
+            __syncthreads();
+            if (a.chunks && n > 0) {
+                const int32_t base = chunk_base;
+                for (int32_t j = tid; j < c; j += SG_SIR_THREADS) a.chunks[base + j] = SgChunk{t, j};
+            }
+        }
         if (STATS && a.segs[tile.seg].stats)
             block_flush4(nS, nI, nR, eS, a.segs[tile.seg].stats + 4 * (int64_t)a.r, red);
+        __syncthreads(); // nch is reset by the next tile
     }
 }
 
 // Warp-synchronous: each warp takes 32 changes of a tile; short transpose rows
 // are updated by their lane, longer ones by the whole warp.
+// ±1 along the transpose rows of one warp's 32 changes of tile t (q0 = first).
+__device__ __forceinline__ void scatter_changes(const SgTickArgs &a, const int32_t *tchanges, int32_t q0,
+                                                int32_t n, int lane)
+{
+    const int32_t q = q0 + lane;
+    const bool valid = q < n;
+    const int32_t c = valid ? tchanges[q] : 0;
+    const int32_t g = c >= 0 ? c : ~c;
+    const int32_t delta = c >= 0 ? 1 : -1;
+    int32_t b = 0, e = 0;
+    if (valid) {
+        b = __ldg(a.toff + g);
+        e = __ldg(a.toff + g + 1);
+    }
+    if (a.rowsegs && e - b > kSegRow) e = b; // handled through the row-segment list
+    const bool long_row = e - b > thread_row_of(a);
+    if (!long_row) {
+        for (int32_t k = b; k < e; k += 4) {
+            const int32_t last = e - 1;
+            const int32_t d0 = __ldg(a.tidx + k);
+            const int32_t d1 = __ldg(a.tidx + min(k + 1, last));
+            const int32_t d2 = __ldg(a.tidx + min(k + 2, last));
+            const int32_t d3 = __ldg(a.tidx + min(k + 3, last));
+            atomicAdd(a.cnt + d0, delta);
+            if (k + 1 < e) atomicAdd(a.cnt + d1, delta);
+            if (k + 2 < e) atomicAdd(a.cnt + d2, delta);
+            if (k + 3 < e) atomicAdd(a.cnt + d3, delta);
+        }
+    }
+    unsigned m = __ballot_sync(FULL_MASK, long_row);
+    while (m) {
+        const int l = __ffs(m) - 1;
+        m &= m - 1;
+        const int32_t hb = __shfl_sync(FULL_MASK, b, l);
+        const int32_t he = __shfl_sync(FULL_MASK, e, l);
+        const int32_t hd = __shfl_sync(FULL_MASK, delta, l);
+        for (int32_t k = hb + lane; k < he; k += 32) atomicAdd(a.cnt + __ldg(a.tidx + k), hd);
+    }
+}
+
+// Work-list form: warps take the tick's non-empty 32-change chunks, so a tile
+// with thousands of changes is spread over many warps.
+__global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_scatter_chunks_kernel(SgTickArgs a)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int32_t nck = a.nchunks[a.r];
+    for (int32_t w = blockIdx.x * kWarps + warp; w < nck; w += gridDim.x * kWarps) {
+        const SgChunk ck = a.chunks[w];
+        scatter_changes(a, a.changes + a.tiles[ck.tile].begin, ck.chunk * 32, __ldg(a.tile_nch + ck.tile), lane);
+    }
+    if (a.rowsegs) {
+        const int32_t nsg = a.nrowsegs[a.r];
+        for (int32_t w = blockIdx.x * kWarps + warp; w < nsg; w += gridDim.x * kWarps) {
+            const SgRowSeg sgm = a.rowsegs[w];
+            for (int32_t k = sgm.begin + lane; k < sgm.end; k += 32) atomicAdd(a.cnt + __ldg(a.tidx + k), sgm.delta);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_scatter_kernel(SgTickArgs a)
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -939,30 +1186,57 @@ cudaError_t sg_launch_sir_count_init(const SgTickArgs &a, int grid, cudaStream_t
     return cudaGetLastError();
 }
 
+template <int V, bool P>
+static void count_step_flavour(const SgTickArgs &a, int flavour, int grid, cudaStream_t st)
+{
+    const bool per8 = flavour & SG_FLAVOUR_PER8, lazy = flavour & SG_FLAVOUR_LAZY;
+    const bool dense = V == 2 && (flavour & SG_FLAVOUR_DENSE);
+#define SG_CF(N, D, L) sir_count_step_kernel<V, false, P, N, D, L><<<grid, SG_SIR_THREADS, 0, st>>>(a)
+    if (per8) {
+        if (dense) {
+            if (lazy) SG_CF(8, true, true); else SG_CF(8, true, false);
+        } else {
+            if (lazy) SG_CF(8, false, true); else SG_CF(8, false, false);
+        }
+    } else {
+        if (dense) {
+            if (lazy) SG_CF(4, true, true); else SG_CF(4, true, false);
+        } else {
+            if (lazy) SG_CF(4, false, true); else SG_CF(4, false, false);
+        }
+    }
+#undef SG_CF
+}
+
 cudaError_t sg_launch_sir_count_step(const SgTickArgs &a, int variant, bool stats, bool inplace,
                                      int grid, cudaStream_t st)
 {
-#define SG_CS(V, S, P) sir_count_step_kernel<V, S, P><<<grid, SG_SIR_THREADS, 0, st>>>(a)
-    if (variant == 1) {
-        if (stats) {
-            if (inplace) SG_CS(1, true, true); else SG_CS(1, true, false);
+    if (stats) { // statistics runs use one flavour
+        if (variant == 1) {
+            if (inplace) sir_count_step_kernel<1, true, true, 4, false, true><<<grid, SG_SIR_THREADS, 0, st>>>(a);
+            else sir_count_step_kernel<1, true, false, 4, false, true><<<grid, SG_SIR_THREADS, 0, st>>>(a);
         } else {
-            if (inplace) SG_CS(1, false, true); else SG_CS(1, false, false);
+            if (inplace) sir_count_step_kernel<2, true, true, 4, true, true><<<grid, SG_SIR_THREADS, 0, st>>>(a);
+            else sir_count_step_kernel<2, true, false, 4, true, true><<<grid, SG_SIR_THREADS, 0, st>>>(a);
         }
-    } else {
-        if (stats) {
-            if (inplace) SG_CS(2, true, true); else SG_CS(2, true, false);
-        } else {
-            if (inplace) SG_CS(2, false, true); else SG_CS(2, false, false);
-        }
+        return cudaGetLastError();
     }
-#undef SG_CS
+    if (variant == 1) {
+        if (inplace) count_step_flavour<1, true>(a, a.flavour, grid, st);
+        else count_step_flavour<1, false>(a, a.flavour, grid, st);
+    } else {
+        if (inplace) count_step_flavour<2, true>(a, a.flavour, grid, st);
+        else count_step_flavour<2, false>(a, a.flavour, grid, st);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t sg_launch_sir_count_scatter(const SgTickArgs &a, int grid, cudaStream_t st)
 {
-    sir_count_scatter_kernel<<<grid, SG_SIR_THREADS, 0, st>>>(a);
+    if (a.chunks)
+        sir_count_scatter_chunks_kernel<<<grid, SG_SIR_THREADS, 0, st>>>(a);
+    else
+        sir_count_scatter_kernel<<<grid, SG_SIR_THREADS, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -39,6 +39,21 @@ struct SgMega {
     int32_t agent, seg;
 };
 
+// Count-step flavours (bit mask; every flavour gives the same result).
+#define SG_FLAVOUR_PER8 1   // 8 agents per thread and pass instead of 4
+#define SG_FLAVOUR_DENSE 2  // warp-dense SIR-B draws
+#define SG_FLAVOUR_LAZY 4   // count and RNG key loaded only where needed
+
+// One warp's share of the scatter: changes [32 * chunk, 32 * chunk + 32) of a tile.
+struct SgChunk {
+    int32_t tile, chunk;
+};
+
+// Part [begin, end) of a changed hub's transpose row, with the change's +-1.
+struct SgRowSeg {
+    int32_t begin, end, delta, pad;
+};
+
 struct SgTickArgs {
     const int32_t *off;     // CSR offsets (global agent index)
     const int32_t *idx;     // CSR indices (global agent index)
@@ -47,6 +62,7 @@ struct SgTickArgs {
     const SgTile *tiles;
     int32_t ntiles;
     int32_t r;              // tick relative to the run start
+    int32_t flavour;        // count-step flavour (SG_FLAVOUR_* bits)
     int32_t thread_row;     // rows up to this length are scanned by one lane, longer
                             // ones by a warp (0 = default 32)
     const SgMega *mega;     // rows longer than mega_row, scanned by whole blocks
@@ -58,6 +74,10 @@ struct SgTickArgs {
     int32_t *changes;       // change list: agent index, ~agent for I->R; tile t
                             // owns changes[tile.begin .. tile.begin + tile_nch[t])
     int32_t *tile_nch;      // [ntiles] changes recorded by each tile this tick
+    SgChunk *chunks;        // NULL, or the scatter's work list of non-empty chunks
+    int32_t *nchunks;       // [ticks] chunk counts, slot r (zero before the run)
+    SgRowSeg *rowsegs;      // NULL, or the scatter's list of long-row segments
+    int32_t *nrowsegs;      // [ticks] segment counts, slot r (zero before the run)
     const int32_t *toff;    // transpose CSR (in-neighbours)
     const int32_t *tidx;
     // frontier strategy

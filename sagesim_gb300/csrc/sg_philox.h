@@ -31,27 +31,47 @@ typedef int int32_t;
 #define SG_PHILOX_M 0xD26275A3u
 #define SG_PHILOX_W 0x9E3779B9u
 
-SG_HD uint32_t sg_mulhi32(uint32_t a, uint32_t b)
-{
-#if defined(__CUDA_ARCH__)
-    return __umulhi(a, b);
-#else
-    return (uint32_t)(((uint64_t)a * (uint64_t)b) >> 32);
-#endif
-}
-
-// Returns the 23-bit Philox integer for counter (c0, c1) and key.
+// Returns the 23-bit Philox integer for counter (c0, c1) and key. Each round is
+// one 32x32->64-bit multiply (both halves at once) and a three-way xor.
 SG_HD uint32_t sg_philox_k23(uint32_t c0, uint32_t c1, uint32_t key)
 {
 #if defined(__CUDA_ARCH__)
 #pragma unroll
 #endif
     for (int r = 0; r < 10; ++r) {
-        const uint32_t hi = sg_mulhi32(c0, SG_PHILOX_M);
-        const uint32_t lo = c0 * SG_PHILOX_M;
-        c0 = hi ^ key ^ c1;
-        c1 = lo;
+        const uint64_t p = (uint64_t)c0 * SG_PHILOX_M;
+        c0 = (uint32_t)(p >> 32) ^ key ^ c1;
+        c1 = (uint32_t)p;
         if (r < 9) key += SG_PHILOX_W;
+    }
+    return c0 & 0x7FFFFFu;
+}
+
+// Round keys key + r * W (r = 0..9) of one seed, computed once and reused by
+// every draw of a kernel that draws many times for the same seed.
+struct SgPhiloxKeys {
+    uint32_t k[10];
+};
+
+SG_HD SgPhiloxKeys sg_philox_keys(uint32_t key)
+{
+    SgPhiloxKeys ks;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int r = 0; r < 10; ++r) ks.k[r] = key + (uint32_t)r * SG_PHILOX_W;
+    return ks;
+}
+
+SG_HD uint32_t sg_philox_k23_keys(uint32_t c0, uint32_t c1, const SgPhiloxKeys &ks)
+{
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p = (uint64_t)c0 * SG_PHILOX_M;
+        c0 = (uint32_t)(p >> 32) ^ ks.k[r] ^ c1;
+        c1 = (uint32_t)p;
     }
     return c0 & 0x7FFFFFu;
 }

@@ -80,3 +80,25 @@ def test_sir_matches_oracle_every_tick(variant, strategy, kind):
             assert np.array_equal(got, ref), "tick %d: %d agents differ" % (t, int((got != ref).sum()))
             assert np.array_equal(stats, rstats), "tick %d stats %s vs %s" % (t, stats, rstats)
             st = ref
+
+
+@pytest.mark.parametrize("flavour", range(8))
+@pytest.mark.parametrize("variant", ["A", "B"])
+def test_count_step_flavours_identical(flavour, variant):
+    """Every count-step flavour (8 agents per thread, warp-dense draws, lazy
+    loads) gives the oracle's states; checked through the non-statistics path."""
+    off, idx = hub_graph(5)
+    n = off.size - 1
+    st0 = _init_state(n, 0.01, 5)
+    with Engine() as e:
+        e.set_graph(off, idx, symmetric=True)
+        e.set_seed(9)
+        p = e.add_property("state", np.int32, init=st0)
+        e.add_sir(p, 0.04, 0.08, variant=variant, strategy="count")
+        e.set_tune(blocks_per_sm=4 + 4 * (flavour & 1), count_flavour=flavour)
+        for t0 in (0, 15, 30):
+            e.run_async(t0, 15, use_graph=(t0 > 0))
+        e.synchronize()
+        got = e.get_property(p)
+    ref, _, _ = oracle.sir_run(1 if variant == "A" else 2, off, idx, st0, 9, 0, 45, 0.04, 0.08)
+    assert np.array_equal(got, ref)
