@@ -403,8 +403,8 @@ def sweep(args):
         eng.add_sir(prop, BETA, GAMMA, variant="B", strategy="count", codes=CODES)
         eng.snapshot()
         ref = None
-        for bps in (4, 8, 16):
-            for fl in range(8):
+        for bps in (8, 16):
+            for fl in (0, 1, 4, 5, 8, 12, 16, 24):
                 eng.set_tune(blocks_per_sm=bps, count_flavour=fl)
                 for _ in range(2):
                     eng.restore()
@@ -437,7 +437,7 @@ def main():
     ap.add_argument("--profile-stats", action="store_true",
                     help="with --profile-case: collect and print per-tick S/I/R/E_S")
     ap.add_argument("--flavour", type=int, default=-1, help="count-step flavour for --profile-case")
-    ap.add_argument("--bps", type=int, default=8, help="blocks per SM for --profile-case")
+    ap.add_argument("--bps", type=int, default=16, help="blocks per SM for --profile-case")
     ap.add_argument("--sweep", action="store_true",
                     help="time every count-step flavour x blocks/SM on the workload and exit")
     ap.add_argument("--no-extras", action="store_true",

@@ -128,9 +128,12 @@ typedef struct sg_tune {
     int32_t blocks_per_sm;     /* persistent grid = blocks_per_sm x SM count     */
     int32_t thread_row;        /* rows up to this length: one lane; longer: warp */
     int32_t mega_row;          /* rows longer than this: a whole block           */
-    int32_t count_flavour;     /* count step: 1 = 8 agents per thread (else 4),  */
-                               /* 2 = warp-dense SIR-B draws, 4 = count and RNG  */
-                               /* key loaded only where needed                   */
+    int32_t count_flavour;     /* count strategy, bit mask (0..31):              */
+                               /*  1 = 8 agents per thread (else 4)              */
+                               /*  2 = warp-dense SIR-B draws                    */
+                               /*  4 = count and RNG key loaded only where needed*/
+                               /*  8 = scatter: one transpose row per lane       */
+                               /* 16 = class sweep (in-place runs)               */
     double us_per_tick;        /* measured by sg_batch_tune (output)             */
 } sg_tune;
 

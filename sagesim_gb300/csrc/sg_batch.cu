@@ -24,6 +24,11 @@ void sg_set_thread_error(const std::string &msg); // sg_engine.cu
 
 namespace {
 constexpr int32_t kLongRowFloor = 512; // rows kept as mega candidates (smallest tunable mega_row)
+// count-step flavours the autotuner times: loop form (4 or 8 agents per thread,
+// eager or lazy loads) and class sweep with the load-balanced scatter, and two
+// of them with the lane-per-row scatter
+constexpr int32_t kCountFlavourCands[] = {0, 1, 4, 5, SG_FLAVOUR_SWEEP, SG_FLAVOUR_ROWSCATTER | 4,
+                                          SG_FLAVOUR_ROWSCATTER | SG_FLAVOUR_SWEEP};
 }
 
 int64_t SgRanges::take(int64_t len)
@@ -67,11 +72,11 @@ int64_t SgRanges::largest() const
 
 int64_t sg_pool_scenario_bytes(int64_t n, int64_t nnz, bool transpose, bool lids)
 {
-    const int64_t per_agent = 4 /*off*/ + 8 /*state x2*/ + 8 /*cnt, changes*/ + (lids ? 4 : 0) +
-                              (transpose ? 4 : 0);
+    const int64_t per_agent = 4 /*off*/ + 8 /*state x2*/ + 8 /*cnt, changes*/ + 2 /*class, activity bit*/ +
+                              (lids ? 4 : 0) + (transpose ? 4 : 0);
     const int64_t per_edge = 4 + (transpose ? 4 : 0);
     const int64_t tiles = (n + SG_TILE - 1) / SG_TILE + 1;
-    return (n + 1) * per_agent + nnz * per_edge + tiles * (int64_t)(sizeof(SgTile) + 4) +
+    return sg_pool_agent_slots(n) * per_agent + nnz * per_edge + tiles * (int64_t)(sizeof(SgTile) + 4) +
            (int64_t)sizeof(SgSeg);
 }
 
@@ -119,6 +124,8 @@ int SgPool::allocate(int64_t acap, int64_t ecap, int64_t max_scen, bool transpos
     all_symmetric = !transpose;
     for (auto &b : st) POOL_CK(b.reserve((size_t)std::max<int64_t>(acap, 1) * 4));
     POOL_CK(cnt.reserve((size_t)std::max<int64_t>(acap, 1) * 4));
+    POOL_CK(cls.reserve(((size_t)acap + 16) & ~size_t(15)));
+    POOL_CK(amask.reserve(((size_t)acap / 32 + 2) * 4));
     POOL_CK(changes.reserve((size_t)std::max<int64_t>(acap, 1) * 4));
     POOL_CK(tile_nch.reserve((size_t)tile_cap * 4));
     POOL_CK(chunks.reserve(((size_t)acap / 32 + (size_t)tile_cap + 1) * sizeof(SgChunk)));
@@ -134,7 +141,7 @@ int SgPool::allocate(int64_t acap, int64_t ecap, int64_t max_scen, bool transpos
 
 bool SgPool::fits(int64_t n, int64_t nnz) const
 {
-    return agents.largest() >= ((n + 1 + 3) & ~int64_t(3)) && (nnz == 0 || edges.largest() >= nnz) &&
+    return agents.largest() >= sg_pool_agent_slots(n) && (nnz == 0 || edges.largest() >= nnz) &&
            (int64_t)scen.size() < seg_cap;
 }
 
@@ -148,9 +155,7 @@ int SgPool::place(const sg_scenario_desc &d, const int32_t *loff, const int32_t 
     if (!sym && all_symmetric) return fail(SG_ERR_INVALID, "pool holds symmetric graphs only");
     if (llids && !any_lids) return fail(SG_ERR_INVALID, "pool was allocated without logical ids");
     if ((int64_t)scen.size() >= seg_cap) return fail(SG_ERR_BUDGET, "scenario table full");
-    // agent slots in multiples of 4 keep every scenario's first agent 16-byte
-    // aligned (128-bit state loads)
-    const int64_t aslots = (n + 1 + 3) & ~int64_t(3);
+    const int64_t aslots = sg_pool_agent_slots(n);
     const int64_t ab = agents.take(aslots);
     if (ab < 0) return fail(SG_ERR_BUDGET, "no room for the scenario's agents");
     const int64_t eb = nnz > 0 ? edges.take(nnz) : 0;
@@ -218,7 +223,7 @@ void SgPool::release(int32_t sid)
     auto it = sid_slot.find(sid);
     if (it == sid_slot.end()) return;
     const size_t slot = it->second;
-    agents.give(scen[slot].agent_base, (scen[slot].n + 1 + 3) & ~int64_t(3));
+    agents.give(scen[slot].agent_base, sg_pool_agent_slots(scen[slot].n));
     if (scen[slot].nnz) edges.give(scen[slot].edge_base, scen[slot].nnz);
     s_long_rows_.erase(sid);
     scen.erase(scen.begin() + (ptrdiff_t)slot);
@@ -315,12 +320,22 @@ int SgPool::enqueue(int32_t nticks, bool capturing)
     a.nrowsegs = nrowsegs.as<int32_t>();
     a.toff = all_symmetric ? off.as<int32_t>() : toff.as<int32_t>();
     a.tidx = all_symmetric ? idx.as<int32_t>() : tidx.as<int32_t>();
+    if (count) {
+        a.cls = cls.as<uint8_t>();
+        a.amask = amask.as<uint32_t>();
+        a.mrebuild = mrebuild.as<uint8_t>();
+        a.tick_changes = tick_changes.as<int32_t>();
+    }
     const int grid = std::max(1, std::min<int>(a.ntiles, sm_count * std::max(tune.blocks_per_sm, 1)));
     const int variant = builtin == SG_BUILTIN_SIR_A ? 1 : 2;
     if (a.ntiles == 0) return SG_OK;
     if (count) {
         POOL_CK(cudaMemsetAsync(nchunks.p, 0, (size_t)nticks * 4, stream));
         POOL_CK(cudaMemsetAsync(nrowsegs.p, 0, (size_t)nticks * 4, stream));
+        // activity bits are not carried between runs: the first sweep of a run rebuilds them
+        POOL_CK(cudaMemsetAsync(mrebuild.p, 0, (size_t)nticks + 1, stream));
+        POOL_CK(cudaMemsetAsync(mrebuild.p, 1, 1, stream));
+        POOL_CK(cudaMemsetAsync(tick_changes.p, 0, (size_t)nticks * 4, stream));
     }
     for (int32_t r = 0; r < nticks; ++r) {
         a.r = r;
@@ -348,6 +363,8 @@ int SgPool::run(int32_t nticks, bool use_graph)
     if (count && nticks > nchunks_cap) { // before any capture: no allocation inside a graph
         POOL_CK(nchunks.reserve((size_t)nticks * 4));
         POOL_CK(nrowsegs.reserve((size_t)nticks * 4));
+        POOL_CK(mrebuild.reserve((size_t)nticks + 1));
+        POOL_CK(tick_changes.reserve((size_t)nticks * 4));
         nchunks_cap = nticks;
     }
     if (count) {
@@ -371,6 +388,8 @@ int SgPool::run(int32_t nticks, bool use_graph)
             a.tiles = itiles.as<SgTile>();
             a.ntiles = (int32_t)init.size();
             a.cnt = cnt.as<int32_t>();
+            a.cls = cls.as<uint8_t>();
+            a.amask = amask.as<uint32_t>();
             a.mega = nullptr;
             a.nmega = 0;
             a.mega_blocks = 0;
@@ -436,6 +455,8 @@ int SgPool::snapshot()
     }
     POOL_CK(snap_cnt.reserve(cnt.bytes));
     POOL_CK(cudaMemcpyAsync(snap_cnt.p, cnt.p, cnt.bytes, cudaMemcpyDeviceToDevice, stream));
+    POOL_CK(snap_cls.reserve(cls.bytes));
+    POOL_CK(cudaMemcpyAsync(snap_cls.p, cls.p, cls.bytes, cudaMemcpyDeviceToDevice, stream));
     snap_host_.clear();
     for (auto &s : scen) snap_host_.push_back({s.tick, s.par, s.cnt_valid});
     POOL_CK(cudaStreamSynchronize(stream));
@@ -449,6 +470,7 @@ int SgPool::restore()
     for (int k = 0; k < 2; ++k)
         POOL_CK(cudaMemcpyAsync(st[k].p, snap_st[k].p, st[k].bytes, cudaMemcpyDeviceToDevice, stream));
     POOL_CK(cudaMemcpyAsync(cnt.p, snap_cnt.p, cnt.bytes, cudaMemcpyDeviceToDevice, stream));
+    POOL_CK(cudaMemcpyAsync(cls.p, snap_cls.p, cls.bytes, cudaMemcpyDeviceToDevice, stream));
     for (size_t k = 0; k < scen.size(); ++k) {
         scen[k].tick = snap_host_[k].tick;
         scen[k].par = snap_host_[k].par;
@@ -473,7 +495,7 @@ size_t SgPool::device_bytes() const
 {
     size_t b = 0;
     for (const SgDev *d : {&off, &idx, &toff, &tidx, &st[0], &st[1], &cnt, &changes, &tile_nch, &lids, &segs,
-                           &tiles, &mega, &snap_st[0], &snap_st[1], &snap_cnt})
+                           &tiles, &mega, &cls, &amask, &snap_st[0], &snap_st[1], &snap_cnt, &snap_cls})
         b += d->bytes;
     return b;
 }
@@ -579,7 +601,7 @@ int sg_batch_commit(sg_batch *b)
     int64_t agents = 0, nnz = 0;
     bool transpose = false, lids = false;
     for (auto &s : b->staged) {
-        agents += (s.d.n_agents + 1 + 3) & ~int64_t(3);
+        agents += sg_pool_agent_slots(s.d.n_agents);
         nnz += s.d.nnz;
         transpose |= !(s.d.flags & SG_GRAPH_SYMMETRIC);
         lids |= !s.lids.empty();
@@ -603,7 +625,7 @@ int sg_batch_set_tune(sg_batch *b, const sg_tune *t)
     if (!b || !t) return SG_ERR_INVALID;
     if (t->strategy != SG_SIR_PULL && t->strategy != SG_SIR_COUNT) return b->pool.fail(SG_ERR_INVALID, "bad strategy");
     if (t->blocks_per_sm < 1 || t->blocks_per_sm > 32 || t->thread_row < 1 || t->mega_row < kLongRowFloor ||
-        t->count_flavour < 0 || t->count_flavour > 7)
+        t->count_flavour < 0 || t->count_flavour > SG_FLAVOUR_MAX)
         return b->pool.fail(SG_ERR_INVALID, "tune parameters out of range");
     const bool mega_changed = t->mega_row != b->pool.tune.mega_row;
     b->pool.tune = *t;
@@ -693,7 +715,7 @@ int sg_batch_tune(sg_batch *b, int32_t ticks, sg_tune *best)
     for (int32_t bps : {2, 4, 8, 16}) {
         for (int32_t trow : {16, 32, 64})
             for (int32_t mrow : {1024, 4096}) cands.push_back(sg_tune{SG_SIR_PULL, bps, trow, mrow, 0, 0.0});
-        for (int32_t fl = 0; fl < 8; ++fl) cands.push_back(sg_tune{SG_SIR_COUNT, bps, 32, 2048, fl, 0.0});
+        for (int32_t fl : kCountFlavourCands) cands.push_back(sg_tune{SG_SIR_COUNT, bps, 32, 2048, fl, 0.0});
     }
     for (sg_tune t : cands) {
         if ((rc = sg_batch_set_tune(b, &t)) != SG_OK) break;

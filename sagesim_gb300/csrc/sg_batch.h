@@ -7,7 +7,8 @@
 //   edge slots   [edge_base, edge_base + nnz): CSR entries as global indices;
 //   state        int32 per agent slot (updated in place by the count strategy;
 //                the pull strategy ping-pongs with a second buffer);
-//   cnt/changes  count-strategy scratch per agent slot;
+//   cnt/changes  count-strategy scratch per agent slot, with the class byte the
+//                class sweep reads;
 //   segs         one SgSeg per scenario (tick counter, horizon, seed, codes);
 //   tiles        the work list of the kernels, tiles never straddle scenarios.
 // Space is handed out first-fit from free lists of agent and edge slots.
@@ -17,6 +18,10 @@
 #include <vector>
 
 #include "sg_internal.h"
+
+// Agent slots of a scenario of n agents: n + 1, rounded up to a multiple of 32
+// (128-bit loads, and class-sweep mask words that belong to one scenario).
+inline int64_t sg_pool_agent_slots(int64_t n) { return (n + 1 + 31) & ~int64_t(31); }
 
 struct SgPoolScen {
     int32_t sid = -1;
@@ -57,9 +62,9 @@ struct SgPool {
     int64_t agent_cap = 0, edge_cap = 0;
     SgRanges agents, edges;
     SgDev off, idx, toff, tidx, st[2], cnt, changes, tile_nch, lids, segs, tiles, mega, chunks, nchunks,
-        rowsegs, nrowsegs;
+        rowsegs, nrowsegs, cls, amask, mrebuild, tick_changes;
     int32_t nchunks_cap = 0;
-    SgDev snap_st[2], snap_cnt;
+    SgDev snap_st[2], snap_cnt, snap_cls;
     bool any_lids = false, all_symmetric = true;
     int64_t seg_cap = 0, tile_cap = 0, mega_cap = 0;
 
@@ -74,7 +79,7 @@ struct SgPool {
     bool tables_dirty = true;
     uint64_t version = 1;
 
-    sg_tune tune{SG_SIR_COUNT, 16, 32, 2048, 0, 0.0};
+    sg_tune tune{SG_SIR_COUNT, 16, 32, 2048, SG_FLAVOUR_SWEEP, 0.0};
     cudaGraphExec_t graph = nullptr;
     int32_t graph_nticks = -1;
     uint64_t graph_version = 0;

@@ -75,13 +75,15 @@ struct sg_engine {
 
     // scratch of the count strategy and of per-tick statistics
     SgDev cnt, changes, tile_nch, stats, chunks, nchunks, rowsegs, nrowsegs;
+    SgDev cls, amask, mrebuild, tick_changes; // class sweep: classes, activity bits, per-tick flags
+    bool cls_on = false; // this run's count step keeps classes (its tiles start at multiples of 32)
     SgDev flist[2], flen, fnch, fmark, fstats_init, fstats_delta; // frontier strategy
     SgDev transpose_tmp, scan_tmp;
     SgDev prop_table; // sg_prop_dev per property, for compiled steps
 
     SgProfiler prof;
     int hub_deg = 32;
-    sg_tune tune{SG_SIR_COUNT, 16, 32, 2048, 0, 0.0};
+    sg_tune tune{SG_SIR_COUNT, 16, 32, 2048, SG_FLAVOUR_SWEEP, 0.0};
     int32_t last_nticks = 0;
 
     // CUDA graph of the tick loop (sg_run_async with use_graph)
@@ -573,6 +575,13 @@ static SgTickArgs base_args(sg_engine *e, SgStep *s, int32_t r, bool inplace)
     a.nchunks = e->nchunks.as<int32_t>();
     a.rowsegs = e->rowsegs.as<SgRowSeg>();
     a.nrowsegs = e->nrowsegs.as<int32_t>();
+    if (e->cls_on && s->bp.strategy == SG_SIR_COUNT &&
+        (s->kind == SG_BUILTIN_SIR_A || s->kind == SG_BUILTIN_SIR_B)) {
+        a.cls = e->cls.as<uint8_t>();
+        a.amask = e->amask.as<uint32_t>();
+        a.mrebuild = e->mrebuild.as<uint8_t>();
+        a.tick_changes = e->tick_changes.as<int32_t>();
+    }
     const bool sym = (e->graph_flags & SG_GRAPH_SYMMETRIC) != 0;
     a.toff = sym ? e->off.as<int32_t>() : e->toff.as<int32_t>();
     a.tidx = sym ? e->idx.as<int32_t>() : e->tidx.as<int32_t>();
@@ -634,6 +643,10 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
         SgTickArgs a = base_args(e, s, 0, pl.count_inplace);
         SG_CK(cudaMemsetAsync(e->nchunks.p, 0, (size_t)std::max(nticks, 1) * 4, e->stream));
         SG_CK(cudaMemsetAsync(e->nrowsegs.p, 0, (size_t)std::max(nticks, 1) * 4, e->stream));
+        if (e->cls_on) { // the init builds exact activity bits: no rebuild at r == 0
+            SG_CK(cudaMemsetAsync(e->mrebuild.p, 0, (size_t)nticks + 1, e->stream));
+            SG_CK(cudaMemsetAsync(e->tick_changes.p, 0, (size_t)std::max(nticks, 1) * 4, e->stream));
+        }
         SG_PROF_LAUNCH("sir_count_init",
                        sg_launch_sir_count_init(a, grid_for(e, s->ntiles) + a.mega_blocks, e->stream));
     }
@@ -742,6 +755,16 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
         SG_CK(e->nchunks.reserve((size_t)std::max(nticks, 1) * 4));
         SG_CK(e->rowsegs.reserve(((size_t)e->nnz / 128 + 64) * sizeof(SgRowSeg)));
         SG_CK(e->nrowsegs.reserve((size_t)std::max(nticks, 1) * 4));
+    }
+    // class bytes and activity bits: kept by every count-strategy kernel, read by
+    // the class sweep; a mask word belongs to one tile only if tiles start at
+    // multiples of 32
+    e->cls_on = pl.count_step && !pl.frontier && pl.count_step->begin % 32 == 0;
+    if (e->cls_on) {
+        SG_CK(e->cls.reserve(((size_t)e->n + 16) & ~size_t(15)));
+        SG_CK(e->amask.reserve(((size_t)e->n / 32 + 2) * 4));
+        SG_CK(e->mrebuild.reserve((size_t)nticks + 1));
+        SG_CK(e->tick_changes.reserve((size_t)std::max(nticks, 1) * 4));
     }
     return SG_OK;
 }
@@ -869,7 +892,7 @@ int sg_engine_set_tune(sg_engine *e, const sg_tune *t)
 {
     if (!e || !t) return SG_ERR_INVALID;
     if (t->blocks_per_sm < 1 || t->blocks_per_sm > 32 || t->thread_row < 1 || t->count_flavour < 0 ||
-        t->count_flavour > 7)
+        t->count_flavour > SG_FLAVOUR_MAX)
         return e->fail(SG_ERR_INVALID, "tune parameters out of range");
     e->tune = *t;
     e->version++;

@@ -1,4 +1,5 @@
-// sg_kernels.cu -- tick kernels for sm_103a.
+// sg_kernels.cu -- pull-strategy, frontier-strategy and opinion tick kernels
+// for sm_103a, and the CSR utilities (placement offsets, transpose).
 //
 // The tick semantics follow SAGESim's generated fused kernel
 // (sagesim/model.py:2306-2408): every step reads tick-start values and writes a
@@ -7,258 +8,15 @@
 // reference's per-tick write-back copy (model.py:2374-2389) disappears.
 //
 // Work decomposition: a persistent grid walks a tile list (tiles never straddle
-// segments). Inside a tile, one thread takes one agent; an agent whose CSR row
-// is longer than hub_deg is pushed to a shared-memory queue and processed by a
-// whole warp after the thread pass (ballot/popc over 32 neighbours per step).
-// That is the degree binning: short rows stay thread-per-agent with no
-// divergence from hubs, hub rows are read coalesced by a warp.
+// segments). Rows are binned by length: a lane scans a row of up to thread_row
+// entries, a warp a row of up to mega_row entries, and rows longer than that
+// are listed at setup and scanned by dedicated blocks. The count strategy's
+// kernels are in sg_count.cu.
 #include <cub/device/device_scan.cuh>
 
-#include "sg_kernels.h"
-#include "sg_philox.h"
-
-#define FULL_MASK 0xffffffffu
+#include "sg_device.cuh"
 
 namespace {
-
-constexpr int kWarps = SG_SIR_THREADS / 32;
-constexpr uint32_t kNormalSalt2 = 73856093u; // sagesim/math_utils.py:252
-
-__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
-    return v;
-}
-
-// Block-reduces four counters and adds them to dst[0..3] (one atomic each).
-__device__ __forceinline__ void block_flush4(unsigned long long v0, unsigned long long v1,
-                                             unsigned long long v2, unsigned long long v3,
-                                             unsigned long long *dst,
-                                             unsigned long long (*sh)[kWarps])
-{
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    v0 = warp_sum(v0);
-    v1 = warp_sum(v1);
-    v2 = warp_sum(v2);
-    v3 = warp_sum(v3);
-    if (lane == 0) {
-        sh[0][warp] = v0;
-        sh[1][warp] = v1;
-        sh[2][warp] = v2;
-        sh[3][warp] = v3;
-    }
-    __syncthreads();
-    if (warp == 0) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            unsigned long long x = lane < kWarps ? sh[k][lane] : 0ull;
-            x = warp_sum(x);
-            if (lane == 0 && x) atomicAdd(dst + k, x);
-        }
-    }
-    __syncthreads();
-}
-
-__device__ __forceinline__ uint32_t seg_lid(const SgSeg &sg, int32_t i)
-{
-    return sg.lids ? __ldg(sg.lids + i) : (uint32_t)(i - sg.lid_base);
-}
-
-// ---- neighbour scans ------------------------------------------------------------
-// Every scan is counted, never ordered: SIR-A needs "any infected neighbour",
-// SIR-B needs only how many of the scanned neighbours are infected (the j-th
-// infected one draws salt 2 + j whichever neighbour it is). So rows are read
-// in batches whose loads are all independent (memory-level parallelism), and
-// the draws for a batch's c infected neighbours are tested together.
-//
-// Three bins by row length, all warp-synchronous: a lane scans its own row
-// when it has <= kThreadRow entries (4 independent gathers per step); the
-// whole warp scans rows of <= kWarpRow entries (128 per step); rows longer
-// than that ("mega" rows, a few dozen in a 10^7-agent power-law graph) are
-// listed at setup and scanned by dedicated blocks (1024 entries per step).
-constexpr int kBatch = 4;
-constexpr int32_t kThreadRow = 32; // default of SgTickArgs::thread_row
-
-__device__ __forceinline__ int32_t thread_row_of(const SgTickArgs &a)
-{
-    return a.thread_row > 0 ? a.thread_row : kThreadRow;
-}
-
-// Number of infected entries among row[k .. min(k+4, e)), e > k.
-__device__ __forceinline__ int batch_count(const int32_t *__restrict__ idx,
-                                           const int32_t *__restrict__ sin, int32_t k, int32_t e,
-                                           int32_t ci)
-{
-    const int32_t last = e - 1;
-    const int32_t n0 = __ldg(idx + k);
-    const int32_t n1 = __ldg(idx + min(k + 1, last));
-    const int32_t n2 = __ldg(idx + min(k + 2, last));
-    const int32_t n3 = __ldg(idx + min(k + 3, last));
-    const int32_t s0 = __ldg(sin + n0), s1 = __ldg(sin + n1), s2 = __ldg(sin + n2),
-                  s3 = __ldg(sin + n3);
-    return (s0 == ci) + (k + 1 < e && s1 == ci) + (k + 2 < e && s2 == ci) + (k + 3 < e && s3 == ci);
-}
-
-// SIR-B outcome for one agent from its row, lane path.
-__device__ __forceinline__ bool trials_thread(const int32_t *__restrict__ idx,
-                                              const int32_t *__restrict__ sin, int32_t b,
-                                              int32_t e, int32_t ci, uint32_t c0b, uint32_t lid,
-                                              uint32_t key, uint32_t kinf)
-{
-    uint32_t j = 0;
-    for (int32_t k = b; k < e; k += kBatch) {
-        const int c = batch_count(idx, sin, k, e, ci);
-        for (int q = 0; q < c; ++q, ++j)
-            if (sg_philox_k23(c0b + 2u + j, lid, key) < kinf) return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ bool any_infected_thread(const int32_t *__restrict__ idx,
-                                                    const int32_t *__restrict__ sin, int32_t b,
-                                                    int32_t e, int32_t ci)
-{
-    for (int32_t k = b; k < e; k += kBatch)
-        if (batch_count(idx, sin, k, e, ci)) return true;
-    return false;
-}
-
-__device__ __forceinline__ int32_t count_thread(const int32_t *__restrict__ idx,
-                                                const int32_t *__restrict__ sin, int32_t b,
-                                                int32_t e, int32_t ci)
-{
-    int32_t c = 0;
-    for (int32_t k = b; k < e; k += kBatch) c += batch_count(idx, sin, k, e, ci);
-    return c;
-}
-
-// Warp path: each lane takes 4 entries per step (128 per warp step).
-__device__ __forceinline__ int warp_batch_count(const int32_t *__restrict__ idx,
-                                                const int32_t *__restrict__ sin, int32_t k0,
-                                                int32_t e, int32_t ci, int lane)
-{
-    const int32_t k = k0 + lane;
-    const bool v0 = k < e, v1 = k + 32 < e, v2 = k + 64 < e, v3 = k + 96 < e;
-    const int32_t last = e - 1;
-    const int32_t n0 = __ldg(idx + min(k, last));
-    const int32_t n1 = __ldg(idx + min(k + 32, last));
-    const int32_t n2 = __ldg(idx + min(k + 64, last));
-    const int32_t n3 = __ldg(idx + min(k + 96, last));
-    const int32_t s0 = __ldg(sin + n0), s1 = __ldg(sin + n1), s2 = __ldg(sin + n2),
-                  s3 = __ldg(sin + n3);
-    int c = (v0 && s0 == ci) + (v1 && s1 == ci) + (v2 && s2 == ci) + (v3 && s3 == ci);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(FULL_MASK, c, o);
-    return c;
-}
-
-// Tests draws j0 .. j0+c-1 (salt 2 + j) across the warp; true if any is below beta.
-__device__ __forceinline__ bool warp_draws(uint32_t j0, int c, uint32_t c0b, uint32_t lid,
-                                           uint32_t key, uint32_t kinf, int lane)
-{
-    for (int q0 = 0; q0 < c; q0 += 32) {
-        const bool ok = (q0 + lane < c) &&
-                        (sg_philox_k23(c0b + 2u + j0 + (uint32_t)(q0 + lane), lid, key) < kinf);
-        if (__any_sync(FULL_MASK, ok)) return true;
-    }
-    return false;
-}
-
-// SIR-B outcome for every lane's agent given its infected-neighbour count k
-// (act = the lane has a susceptible agent with k > 0). Each lane tests its
-// first kLaneDraws draws itself; agents that need more share the warp, which
-// tests 32 draws (salt 2 + j) per step. Every lane of the warp must call it.
-constexpr int32_t kLaneDraws = 2;
-
-__device__ __forceinline__ bool sirb_infected(bool act, int32_t k, uint32_t c0b, uint32_t lid,
-                                              uint32_t key, uint32_t kinf, int lane)
-{
-    bool inf = false;
-    int32_t done = 0;
-    if (act) {
-        done = k < kLaneDraws ? k : kLaneDraws;
-        for (int32_t j = 0; j < done; ++j)
-            if (sg_philox_k23(c0b + 2u + (uint32_t)j, lid, key) < kinf) {
-                inf = true;
-                break;
-            }
-    }
-    unsigned m = __ballot_sync(FULL_MASK, act && !inf && k > done);
-    while (m) {
-        const int l = __ffs(m) - 1;
-        m &= m - 1;
-        const int32_t bk = __shfl_sync(FULL_MASK, k, l);
-        const uint32_t bc = __shfl_sync(FULL_MASK, c0b, l);
-        const uint32_t bl = __shfl_sync(FULL_MASK, lid, l);
-        const uint32_t bkey = __shfl_sync(FULL_MASK, key, l);
-        const uint32_t bkinf = __shfl_sync(FULL_MASK, kinf, l);
-        const bool hit = warp_draws((uint32_t)kLaneDraws, bk - kLaneDraws, bc, bl, bkey, bkinf, lane);
-        if (lane == l) inf = hit;
-    }
-    return inf;
-}
-
-// VARIANT 1: any infected; 2: SIR-B trials; 0: count (returned through *count).
-template <int VARIANT>
-__device__ __forceinline__ bool warp_row(const int32_t *__restrict__ idx,
-                                         const int32_t *__restrict__ sin, int32_t b, int32_t e,
-                                         int32_t ci, uint32_t c0b, uint32_t lid, uint32_t key,
-                                         uint32_t kinf, int lane, int32_t *count)
-{
-    uint32_t j = 0;
-    for (int32_t k0 = b; k0 < e; k0 += 128) {
-        const int c = warp_batch_count(idx, sin, k0, e, ci, lane);
-        if (VARIANT == 1 && c) return true;
-        if (VARIANT == 2 && c) {
-            if (warp_draws(j, c, c0b, lid, key, kinf, lane)) return true;
-        }
-        j += (uint32_t)c;
-    }
-    if (count) *count = (int32_t)j;
-    return false;
-}
-
-// Block path for mega rows: 256 threads x 4 entries per step; the result is
-// broadcast through __syncthreads_or / a shared counter. Called by every
-// thread of the block.
-template <int VARIANT>
-__device__ __forceinline__ bool block_row(const int32_t *__restrict__ idx,
-                                          const int32_t *__restrict__ sin, int32_t b, int32_t e,
-                                          int32_t ci, uint32_t c0b, uint32_t lid, uint32_t key,
-                                          uint32_t kinf, int32_t *sh_count, int32_t *count)
-{
-    const int tid = threadIdx.x;
-    __syncthreads(); // previous users of *sh_count are done
-    if (tid == 0) *sh_count = 0;
-    __syncthreads();
-    for (int32_t k0 = b; k0 < e; k0 += 4 * SG_SIR_THREADS) {
-        const int32_t k = k0 + tid;
-        const int32_t last = e - 1;
-        const int32_t n0 = __ldg(idx + min(k, last));
-        const int32_t n1 = __ldg(idx + min(k + SG_SIR_THREADS, last));
-        const int32_t n2 = __ldg(idx + min(k + 2 * SG_SIR_THREADS, last));
-        const int32_t n3 = __ldg(idx + min(k + 3 * SG_SIR_THREADS, last));
-        const int mine = (k < e && __ldg(sin + n0) == ci) +
-                         (k + SG_SIR_THREADS < e && __ldg(sin + n1) == ci) +
-                         (k + 2 * SG_SIR_THREADS < e && __ldg(sin + n2) == ci) +
-                         (k + 3 * SG_SIR_THREADS < e && __ldg(sin + n3) == ci);
-        if (mine) atomicAdd(sh_count, mine);
-        if (VARIANT == 1) {
-            if (__syncthreads_or(mine != 0)) return true;
-        }
-    }
-    __syncthreads();
-    const int32_t total = *sh_count;
-    if (count) *count = total;
-    if (VARIANT == 2) {
-        bool ok = false;
-        for (int32_t q = tid; q < total && !ok; q += SG_SIR_THREADS)
-            ok = sg_philox_k23(c0b + 2u + (uint32_t)q, lid, key) < kinf;
-        return __syncthreads_or(ok) != 0;
-    }
-    return false;
-}
 
 // ---- pull strategy --------------------------------------------------------------
 // Blocks [0, gridDim.x - a.mega_blocks) walk the tiles, one warp per 32
@@ -371,477 +129,6 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_pull_kernel(SgTickArgs a)
             }
         }
         if (STATS && sg.stats) block_flush4(nS, nI, nR, eS, sg.stats + 4 * (int64_t)a.r, red);
-    }
-}
-
-// ---- count strategy -------------------------------------------------------------
-// cnt[i] = number of infected agents in row i, kept for susceptible agents
-// (the only ones that read it; agents never return to S). A susceptible agent
-// then needs only cnt[i]: SIR-A infects iff cnt > 0 and u < beta, SIR-B iff
-// one of the draws salt 2 .. 2+cnt-1 is below beta. Agents whose infected
-// status changed are appended to their tile's slice of the change list
-// (tile t owns changes[tile.begin ..] and tile_nch[t]; no global atomics);
-// the scatter kernel then adds +-1 to cnt along their transpose rows.
-
-__global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_init_kernel(SgTickArgs a)
-{
-    __shared__ int32_t sh_count;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int tile_blocks = (int)gridDim.x - a.mega_blocks;
-    if ((int)blockIdx.x >= tile_blocks) {
-        for (int q = (int)blockIdx.x - tile_blocks; q < a.nmega; q += a.mega_blocks) {
-            const SgMega mg = a.mega[q];
-            const SgSeg &sg = a.segs[mg.seg];
-            const int32_t *__restrict__ sin = (const int32_t *)((sg.par0 & 1) ? a.buf1 : a.buf0);
-            const int32_t h = mg.agent;
-            if (sin[h] != sg.cs) continue;
-            int32_t c = 0;
-            block_row<0>(a.idx, sin, a.off[h], a.off[h + 1], sg.ci, 0, 0, 0, 0, &sh_count, &c);
-            if (tid == 0) a.cnt[h] = c;
-        }
-        return;
-    }
-    for (int t = blockIdx.x; t < a.ntiles; t += tile_blocks) {
-        const SgTile tile = a.tiles[t];
-        const SgSeg &sg = a.segs[tile.seg];
-        const int32_t *__restrict__ sin = (const int32_t *)((sg.par0 & 1) ? a.buf1 : a.buf0);
-        const int32_t ci = sg.ci, cs = sg.cs;
-        for (int32_t wbase = tile.begin + warp * 32; wbase < tile.end; wbase += SG_SIR_THREADS) {
-            const int32_t i = wbase + lane;
-            bool medium = false;
-            int32_t b = 0, e = 0;
-            if (i < tile.end && sin[i] == cs) {
-                b = a.off[i];
-                e = a.off[i + 1];
-                if (e - b > a.mega_row) {
-                    // mega block
-                } else if (e - b > thread_row_of(a)) {
-                    medium = true;
-                } else {
-                    a.cnt[i] = count_thread(a.idx, sin, b, e, ci);
-                }
-            }
-            unsigned m = __ballot_sync(FULL_MASK, medium);
-            while (m) {
-                const int l = __ffs(m) - 1;
-                m &= m - 1;
-                const int32_t hb = __shfl_sync(FULL_MASK, b, l);
-                const int32_t he = __shfl_sync(FULL_MASK, e, l);
-                int32_t c = 0;
-                warp_row<0>(a.idx, sin, hb, he, ci, 0, 0, 0, 0, lane, &c);
-                if (lane == l) a.cnt[i] = c;
-            }
-        }
-    }
-}
-
-constexpr int kPerThread = SG_TILE / SG_SIR_THREADS; // agents per thread in a tile
-
-// Warp-dense SIR-B draws. Lane l holds up to kCountPer susceptible agents; agent
-// q needs draws j = 0 .. k[q]-1 (salt 2 + j) until one is below beta. The warp
-// lays out the first min(k, kWarpDenseCap) draws of all its agents in one
-// sequence (exclusive scan of the lanes' totals) and evaluates 32 of them per
-// step, one per lane: the owner of draw d is found by a shuffle binary search
-// over the lanes' scan values. Hits are flagged in shared memory. Agents with
-// more draws and no hit continue with 32-wide warp batches. Returns the bit
-// mask of the calling lane's infected agents. Every lane must call it.
-constexpr int32_t kWarpDenseCap = 32;
-
-template <int P>
-__device__ __forceinline__ unsigned warp_dense_sirb(const int32_t (&k)[P], const uint32_t (&lid)[P],
-                                                    uint32_t c0b, uint32_t key, uint32_t kinf, int lane,
-                                                    unsigned char *flags /* 32 * P bytes of this warp */)
-{
-    int32_t c[P], tot = 0;
-#pragma unroll
-    for (int q = 0; q < P; ++q) {
-        c[q] = k[q] < kWarpDenseCap ? k[q] : kWarpDenseCap;
-        tot += c[q];
-        flags[lane * P + q] = 0;
-    }
-    int32_t x = tot;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int32_t y = __shfl_up_sync(FULL_MASK, x, o);
-        if (lane >= o) x += y;
-    }
-    const int32_t base = x - tot;
-    const int32_t W = __shfl_sync(FULL_MASK, x, 31);
-    __syncwarp();
-    for (int32_t d0 = 0; d0 < W; d0 += 32) {
-        const int32_t d = d0 + lane;
-        int32_t lo = 0; // owner: the last lane with base <= d
-#pragma unroll
-        for (int step = 16; step >= 1; step >>= 1) {
-            const int32_t b = __shfl_sync(FULL_MASK, base, (lo + step) & 31);
-            if (lo + step < 32 && b <= d) lo += step;
-        }
-        int32_t off = d - __shfl_sync(FULL_MASK, base, lo);
-        int32_t qsel = 0;
-        uint32_t l = 0;
-#pragma unroll
-        for (int q = 0; q < P; ++q) {
-            const int32_t cq = __shfl_sync(FULL_MASK, c[q], lo);
-            const uint32_t lq = __shfl_sync(FULL_MASK, lid[q], lo);
-            if (qsel == q) {
-                if (off < cq) {
-                    l = lq;
-                    qsel = q + 100; // found: stop advancing
-                } else {
-                    off -= cq;
-                    qsel = q + 1;
-                }
-            }
-        }
-        if (d < W && qsel >= 100 && sg_philox_k23(c0b + 2u + (uint32_t)off, l, key) < kinf)
-            flags[lo * P + (qsel - 100)] = 1;
-    }
-    __syncwarp();
-    unsigned bits = 0;
-#pragma unroll
-    for (int q = 0; q < P; ++q) {
-        bool inf = flags[lane * P + q] != 0;
-        unsigned m = __ballot_sync(FULL_MASK, !inf && k[q] > kWarpDenseCap);
-        while (m) {
-            const int src = __ffs(m) - 1;
-            m &= m - 1;
-            const int32_t bk = __shfl_sync(FULL_MASK, k[q], src);
-            const uint32_t bl = __shfl_sync(FULL_MASK, lid[q], src);
-            const bool h = warp_draws((uint32_t)kWarpDenseCap, bk - kWarpDenseCap, c0b, bl, key, kinf, lane);
-            if (lane == src) inf = h;
-        }
-        if (inf) bits |= 1u << q;
-    }
-    __syncwarp(); // flags are reused by the next call
-    return bits;
-}
-
-// A changed agent whose transpose row is longer than kSegRow is handed to the
-// scatter as row segments of kSegRow entries on their own work list, so no
-// single warp walks a hub's whole row; the chunk pass skips such rows.
-constexpr int32_t kSegRow = 256;
-
-__device__ __forceinline__ void publish_long_row(const SgTickArgs &a, int32_t g, int32_t delta)
-{
-    const int32_t b = __ldg(a.toff + g), e = __ldg(a.toff + g + 1);
-    if (e - b <= kSegRow) return;
-    const int32_t nseg = (e - b + kSegRow - 1) / kSegRow;
-    const int32_t base = atomicAdd(a.nrowsegs + a.r, nseg);
-    for (int32_t j = 0; j < nseg; ++j) {
-        const int32_t sb = b + j * kSegRow;
-        a.rowsegs[base + j] = SgRowSeg{sb, min(sb + kSegRow, e), delta, 0};
-    }
-}
-
-// Count-strategy step. Late in an epidemic this is a streaming pass over every
-// agent; at its peak most susceptible agents draw. Flavours (all give the
-// same result; the autotuner picks one):
-//   PER    4: one agent per thread per 256-agent stripe (scalar loads); 8: two
-//          runs of 4 consecutive agents per thread read with 128-bit loads
-//   DENSE  SIR-B draws laid out warp-densely (warp_dense_sirb) instead of per-lane loops
-//   LAZY   the count and RNG key are loaded only for agents that need them (a
-//          second round trip) instead of unconditionally with the state
-// The segment's parameters stay in registers while consecutive tiles share a
-// segment, and changes go to the tile's own slice of the change list.
-template <int VARIANT, bool STATS, bool INPLACE, int PER, bool DENSE, bool LAZY>
-__global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickArgs a)
-{
-    static_assert(SG_TILE % (SG_SIR_THREADS * PER) == 0, "tile must be whole passes");
-    __shared__ unsigned long long red[4][kWarps];
-    __shared__ int32_t nch, chunk_base;
-    __shared__ unsigned char wflags[DENSE ? SG_SIR_THREADS * PER : 1];
-    const int tid = threadIdx.x, lane = tid & 31;
-    int32_t cur_seg = -1;
-    int64_t tick = 0, end_tick = 0;
-    uint32_t c0b = 0, key = 0, kinf = 0, krec = 0;
-    int32_t cs = 0, ci = 0, cr = 0, par = 0, lid_base = 0;
-    const uint32_t *lids = nullptr;
-    SgPhiloxKeys ks = sg_philox_keys(0);
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-        const SgTile tile = a.tiles[t];
-        if (tile.seg != cur_seg) {
-            const SgSeg &sg = a.segs[tile.seg];
-            cur_seg = tile.seg;
-            tick = sg.tick0 + a.r;
-            end_tick = sg.end_tick;
-            c0b = sg_c0base(tick);
-            key = sg.key;
-            ks = sg_philox_keys(key);
-            kinf = sg.kinf;
-            krec = sg.krec;
-            cs = sg.cs;
-            ci = sg.ci;
-            cr = sg.cr;
-            par = INPLACE ? 0 : ((sg.par0 + a.r) & 1);
-            lids = sg.lids;
-            lid_base = sg.lid_base;
-        }
-        if (tick >= end_tick) {
-            if (tid == 0) a.tile_nch[t] = 0;
-            continue;
-        }
-        const int32_t *sin = (const int32_t *)(par ? a.buf1 : a.buf0);
-        int32_t *sout = (int32_t *)(INPLACE ? a.buf0 : (par ? a.buf0 : a.buf1));
-        int32_t *tchanges = a.changes + tile.begin;
-        unsigned long long nS = 0, nI = 0, nR = 0, eS = 0;
-        if (tid == 0) nch = 0;
-        __syncthreads();
-        for (int32_t pass = tile.begin; pass < tile.end; pass += SG_SIR_THREADS * PER) {
-            // agent of slot q: PER == 4 -> strided (pass + q*256 + tid, scalar
-            // coalesced loads); PER == 8 -> two runs of 4 consecutive agents per
-            // thread (pass + (q/4)*1024 + tid*4 + q%4) read with 128-bit loads
-            auto agent = [&](int q) -> int32_t {
-                return PER == 8 ? pass + (q >> 2) * (SG_SIR_THREADS * 4) + tid * 4 + (q & 3)
-                                : pass + q * SG_SIR_THREADS + tid;
-            };
-            int32_t s[PER], k[PER];
-            uint32_t lid[PER];
-            if (PER == 8) {
-#pragma unroll
-                for (int g = 0; g < 2; ++g) {
-                    const int32_t b = agent(g * 4);
-                    if (b + 3 < tile.end && (b & 3) == 0) {
-                        const int4 v = *reinterpret_cast<const int4 *>(sin + b);
-                        s[g * 4] = v.x;
-                        s[g * 4 + 1] = v.y;
-                        s[g * 4 + 2] = v.z;
-                        s[g * 4 + 3] = v.w;
-                        if (!LAZY) {
-                            const int4 c = *reinterpret_cast<const int4 *>(a.cnt + b);
-                            k[g * 4] = c.x;
-                            k[g * 4 + 1] = c.y;
-                            k[g * 4 + 2] = c.z;
-                            k[g * 4 + 3] = c.w;
-                            if (lids) {
-                                const uint4 l = __ldg(reinterpret_cast<const uint4 *>(lids + b));
-                                lid[g * 4] = l.x;
-                                lid[g * 4 + 1] = l.y;
-                                lid[g * 4 + 2] = l.z;
-                                lid[g * 4 + 3] = l.w;
-                            } else {
-#pragma unroll
-                                for (int e = 0; e < 4; ++e) lid[g * 4 + e] = (uint32_t)(b + e - lid_base);
-                            }
-                        }
-                    } else {
-#pragma unroll
-                        for (int e = 0; e < 4; ++e) {
-                            const int32_t i = b + e;
-                            const bool v = i < tile.end;
-                            s[g * 4 + e] = v ? sin[i] : INT32_MIN;
-                            if (!LAZY) {
-                                k[g * 4 + e] = v ? a.cnt[i] : 0;
-                                lid[g * 4 + e] = lids ? (v ? __ldg(lids + i) : 0u) : (uint32_t)(i - lid_base);
-                            }
-                        }
-                    }
-                }
-            } else {
-#pragma unroll
-                for (int q = 0; q < PER; ++q) {
-                    const int32_t i = agent(q);
-                    const bool v = i < tile.end;
-                    s[q] = v ? sin[i] : INT32_MIN;
-                    if (!LAZY) {
-                        k[q] = v ? a.cnt[i] : 0;
-                        lid[q] = lids ? (v ? __ldg(lids + i) : 0u) : (uint32_t)(i - lid_base);
-                    }
-                }
-            }
-            if (LAZY) {
-#pragma unroll
-                for (int q = 0; q < PER; ++q) k[q] = s[q] == cs ? a.cnt[agent(q)] : 0;
-#pragma unroll
-                for (int q = 0; q < PER; ++q) {
-                    const int32_t i = agent(q);
-                    lid[q] = (s[q] == ci || (s[q] == cs && k[q] > 0))
-                                 ? (lids ? __ldg(lids + i) : (uint32_t)(i - lid_base))
-                                 : 0u;
-                }
-            }
-            unsigned inf_bits = 0;
-            if (VARIANT == 2 && DENSE) {
-                int32_t kd[PER];
-#pragma unroll
-                for (int q = 0; q < PER; ++q) kd[q] = s[q] == cs ? k[q] : 0;
-                inf_bits = warp_dense_sirb<PER>(kd, lid, c0b, key, kinf, lane, wflags + (tid >> 5) * 32 * PER);
-            }
-#pragma unroll
-            for (int q = 0; q < PER; ++q) {
-                const int32_t i = agent(q);
-                int32_t out = s[q];
-                bool has = false;
-                int32_t code = 0;
-                if (s[q] == ci) {
-                    if (sg_philox_k23_keys(c0b + 1u, lid[q], ks) < krec) {
-                        out = cr;
-                        has = true;
-                        code = ~i;
-                    }
-                } else if (s[q] == cs && k[q] > 0) {
-                    bool inf = false;
-                    if (VARIANT == 1) {
-                        inf = sg_philox_k23_keys(c0b + 1u, lid[q], ks) < kinf;
-                    } else if (DENSE) {
-                        inf = ((inf_bits >> q) & 1u) != 0;
-                    } else {
-                        for (int32_t j = 0; j < k[q]; ++j)
-                            if (sg_philox_k23_keys(c0b + 2u + (uint32_t)j, lid[q], ks) < kinf) {
-                                inf = true;
-                                break;
-                            }
-                    }
-                    if (inf) {
-                        out = ci;
-                        has = true;
-                        code = i;
-                    }
-                }
-                if (i < tile.end) {
-                    if (!INPLACE || has) sout[i] = out;
-                    if (STATS) {
-                        if (s[q] == cs) eS += (unsigned long long)(__ldg(a.off + i + 1) - __ldg(a.off + i));
-                        nS += (out == cs);
-                        nI += (out == ci);
-                        nR += (out == cr);
-                    }
-                }
-                const unsigned m = __ballot_sync(FULL_MASK, has);
-                if (m) {
-                    const int leader = __ffs(m) - 1;
-                    int32_t pos = 0;
-                    if (lane == leader) pos = atomicAdd(&nch, __popc(m));
-                    pos = __shfl_sync(FULL_MASK, pos, leader);
-                    if (has) tchanges[pos + __popc(m & ((1u << lane) - 1u))] = code;
-                }
-                if (has && a.rowsegs) publish_long_row(a, i, code >= 0 ? 1 : -1);
-            }
-        }
-        __syncthreads();
-        {
-            // publish the tile's change count and its 32-change chunks to the
-            // scatter's work list (one atomic per tile with changes)
-            const int32_t n = nch;
-            const int32_t c = (n + 31) >> 5;
-            if (tid == 0) {
-                a.tile_nch[t] = n;
-                if (a.chunks && n > 0) chunk_base = atomicAdd(a.nchunks + a.r, c);
-            }
-            __syncthreads();
-            if (a.chunks && n > 0) {
-                const int32_t base = chunk_base;
-                for (int32_t j = tid; j < c; j += SG_SIR_THREADS) a.chunks[base + j] = SgChunk{t, j};
-            }
-        }
-        if (STATS && a.segs[tile.seg].stats)
-            block_flush4(nS, nI, nR, eS, a.segs[tile.seg].stats + 4 * (int64_t)a.r, red);
-        __syncthreads(); // nch is reset by the next tile
-    }
-}
-
-// Warp-synchronous: each warp takes 32 changes of a tile; short transpose rows
-// are updated by their lane, longer ones by the whole warp.
-// ±1 along the transpose rows of one warp's 32 changes of tile t (q0 = first).
-__device__ __forceinline__ void scatter_changes(const SgTickArgs &a, const int32_t *tchanges, int32_t q0,
-                                                int32_t n, int lane)
-{
-    const int32_t q = q0 + lane;
-    const bool valid = q < n;
-    const int32_t c = valid ? tchanges[q] : 0;
-    const int32_t g = c >= 0 ? c : ~c;
-    const int32_t delta = c >= 0 ? 1 : -1;
-    int32_t b = 0, e = 0;
-    if (valid) {
-        b = __ldg(a.toff + g);
-        e = __ldg(a.toff + g + 1);
-    }
-    if (a.rowsegs && e - b > kSegRow) e = b; // handled through the row-segment list
-    const bool long_row = e - b > thread_row_of(a);
-    if (!long_row) {
-        for (int32_t k = b; k < e; k += 4) {
-            const int32_t last = e - 1;
-            const int32_t d0 = __ldg(a.tidx + k);
-            const int32_t d1 = __ldg(a.tidx + min(k + 1, last));
-            const int32_t d2 = __ldg(a.tidx + min(k + 2, last));
-            const int32_t d3 = __ldg(a.tidx + min(k + 3, last));
-            atomicAdd(a.cnt + d0, delta);
-            if (k + 1 < e) atomicAdd(a.cnt + d1, delta);
-            if (k + 2 < e) atomicAdd(a.cnt + d2, delta);
-            if (k + 3 < e) atomicAdd(a.cnt + d3, delta);
-        }
-    }
-    unsigned m = __ballot_sync(FULL_MASK, long_row);
-    while (m) {
-        const int l = __ffs(m) - 1;
-        m &= m - 1;
-        const int32_t hb = __shfl_sync(FULL_MASK, b, l);
-        const int32_t he = __shfl_sync(FULL_MASK, e, l);
-        const int32_t hd = __shfl_sync(FULL_MASK, delta, l);
-        for (int32_t k = hb + lane; k < he; k += 32) atomicAdd(a.cnt + __ldg(a.tidx + k), hd);
-    }
-}
-
-// Work-list form: warps take the tick's non-empty 32-change chunks, so a tile
-// with thousands of changes is spread over many warps.
-__global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_scatter_chunks_kernel(SgTickArgs a)
-{
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int32_t nck = a.nchunks[a.r];
-    for (int32_t w = blockIdx.x * kWarps + warp; w < nck; w += gridDim.x * kWarps) {
-        const SgChunk ck = a.chunks[w];
-        scatter_changes(a, a.changes + a.tiles[ck.tile].begin, ck.chunk * 32, __ldg(a.tile_nch + ck.tile), lane);
-    }
-    if (a.rowsegs) {
-        const int32_t nsg = a.nrowsegs[a.r];
-        for (int32_t w = blockIdx.x * kWarps + warp; w < nsg; w += gridDim.x * kWarps) {
-            const SgRowSeg sgm = a.rowsegs[w];
-            for (int32_t k = sgm.begin + lane; k < sgm.end; k += 32) atomicAdd(a.cnt + __ldg(a.tidx + k), sgm.delta);
-        }
-    }
-}
-
-__global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_scatter_kernel(SgTickArgs a)
-{
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-        const int32_t n = a.tile_nch[t];
-        if (n == 0) continue;
-        const int32_t *tchanges = a.changes + a.tiles[t].begin;
-        for (int32_t q0 = warp * 32; q0 < n; q0 += SG_SIR_THREADS) {
-            const int32_t q = q0 + lane;
-            const bool valid = q < n;
-            const int32_t c = valid ? tchanges[q] : 0;
-            const int32_t g = c >= 0 ? c : ~c;
-            const int32_t delta = c >= 0 ? 1 : -1;
-            int32_t b = 0, e = 0;
-            if (valid) {
-                b = __ldg(a.toff + g);
-                e = __ldg(a.toff + g + 1);
-            }
-            const bool long_row = e - b > thread_row_of(a);
-            if (!long_row) {
-                for (int32_t k = b; k < e; k += 4) {
-                    const int32_t last = e - 1;
-                    const int32_t d0 = __ldg(a.tidx + k);
-                    const int32_t d1 = __ldg(a.tidx + min(k + 1, last));
-                    const int32_t d2 = __ldg(a.tidx + min(k + 2, last));
-                    const int32_t d3 = __ldg(a.tidx + min(k + 3, last));
-                    atomicAdd(a.cnt + d0, delta);
-                    if (k + 1 < e) atomicAdd(a.cnt + d1, delta);
-                    if (k + 2 < e) atomicAdd(a.cnt + d2, delta);
-                    if (k + 3 < e) atomicAdd(a.cnt + d3, delta);
-                }
-            }
-            unsigned m = __ballot_sync(FULL_MASK, long_row);
-            while (m) {
-                const int l = __ffs(m) - 1;
-                m &= m - 1;
-                const int32_t hb = __shfl_sync(FULL_MASK, b, l);
-                const int32_t he = __shfl_sync(FULL_MASK, e, l);
-                const int32_t hd = __shfl_sync(FULL_MASK, delta, l);
-                for (int32_t k = hb + lane; k < he; k += 32) atomicAdd(a.cnt + __ldg(a.tidx + k), hd);
-            }
-        }
     }
 }
 
@@ -1177,66 +464,6 @@ cudaError_t sg_launch_sir_pull(const SgTickArgs &a, int variant, bool stats, int
         else
             sir_pull_kernel<2, false><<<grid, SG_SIR_THREADS, 0, st>>>(a);
     }
-    return cudaGetLastError();
-}
-
-cudaError_t sg_launch_sir_count_init(const SgTickArgs &a, int grid, cudaStream_t st)
-{
-    sir_count_init_kernel<<<grid, SG_SIR_THREADS, 0, st>>>(a);
-    return cudaGetLastError();
-}
-
-template <int V, bool P>
-static void count_step_flavour(const SgTickArgs &a, int flavour, int grid, cudaStream_t st)
-{
-    const bool per8 = flavour & SG_FLAVOUR_PER8, lazy = flavour & SG_FLAVOUR_LAZY;
-    const bool dense = V == 2 && (flavour & SG_FLAVOUR_DENSE);
-#define SG_CF(N, D, L) sir_count_step_kernel<V, false, P, N, D, L><<<grid, SG_SIR_THREADS, 0, st>>>(a)
-    if (per8) {
-        if (dense) {
-            if (lazy) SG_CF(8, true, true); else SG_CF(8, true, false);
-        } else {
-            if (lazy) SG_CF(8, false, true); else SG_CF(8, false, false);
-        }
-    } else {
-        if (dense) {
-            if (lazy) SG_CF(4, true, true); else SG_CF(4, true, false);
-        } else {
-            if (lazy) SG_CF(4, false, true); else SG_CF(4, false, false);
-        }
-    }
-#undef SG_CF
-}
-
-cudaError_t sg_launch_sir_count_step(const SgTickArgs &a, int variant, bool stats, bool inplace,
-                                     int grid, cudaStream_t st)
-{
-    if (stats) { // statistics runs use one flavour
-        if (variant == 1) {
-            if (inplace) sir_count_step_kernel<1, true, true, 4, false, true><<<grid, SG_SIR_THREADS, 0, st>>>(a);
-            else sir_count_step_kernel<1, true, false, 4, false, true><<<grid, SG_SIR_THREADS, 0, st>>>(a);
-        } else {
-            if (inplace) sir_count_step_kernel<2, true, true, 4, true, true><<<grid, SG_SIR_THREADS, 0, st>>>(a);
-            else sir_count_step_kernel<2, true, false, 4, true, true><<<grid, SG_SIR_THREADS, 0, st>>>(a);
-        }
-        return cudaGetLastError();
-    }
-    if (variant == 1) {
-        if (inplace) count_step_flavour<1, true>(a, a.flavour, grid, st);
-        else count_step_flavour<1, false>(a, a.flavour, grid, st);
-    } else {
-        if (inplace) count_step_flavour<2, true>(a, a.flavour, grid, st);
-        else count_step_flavour<2, false>(a, a.flavour, grid, st);
-    }
-    return cudaGetLastError();
-}
-
-cudaError_t sg_launch_sir_count_scatter(const SgTickArgs &a, int grid, cudaStream_t st)
-{
-    if (a.chunks)
-        sir_count_scatter_chunks_kernel<<<grid, SG_SIR_THREADS, 0, st>>>(a);
-    else
-        sir_count_scatter_kernel<<<grid, SG_SIR_THREADS, 0, st>>>(a);
     return cudaGetLastError();
 }
 

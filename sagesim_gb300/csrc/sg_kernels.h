@@ -43,6 +43,10 @@ struct SgMega {
 #define SG_FLAVOUR_PER8 1   // 8 agents per thread and pass instead of 4
 #define SG_FLAVOUR_DENSE 2  // warp-dense SIR-B draws
 #define SG_FLAVOUR_LAZY 4   // count and RNG key loaded only where needed
+#define SG_FLAVOUR_ROWSCATTER 8 // scatter walks one transpose row per lane instead of
+                                // the warp's rows laid end to end
+#define SG_FLAVOUR_SWEEP 16 // class sweep (in-place runs that keep class bytes)
+#define SG_FLAVOUR_MAX 31
 
 // One warp's share of the scatter: changes [32 * chunk, 32 * chunk + 32) of a tile.
 struct SgChunk {
@@ -80,6 +84,18 @@ struct SgTickArgs {
     int32_t *nrowsegs;      // [ticks] segment counts, slot r (zero before the run)
     const int32_t *toff;    // transpose CSR (in-neighbours)
     const int32_t *tidx;
+    uint8_t *cls;           // NULL, or per agent its class (0 S, 1 I, 2 R, 3 other),
+                            // kept in step with the state by every count kernel;
+                            // tiles then start at multiples of 32
+    uint32_t *amask;        // with cls: bit i set whenever cnt[i] may be > 0 (set by
+                            // the init and by the scatter's +1, cleared by the sweep
+                            // when it reads 0)
+    uint8_t *mrebuild;      // NULL, or [ticks + 1] flags: 1 = the activity bits are not
+                            // kept for tick r (the scatter of tick r - 1 had too many
+                            // changes to set them), so the sweep of tick r rebuilds
+                            // them from the counts; zero before the run
+    int32_t *tick_changes;  // with mrebuild: [ticks] changes recorded by the sweep at
+                            // tick r (zero before the run)
     // frontier strategy
     int32_t *list[2];       // active agents of tick r in list[r & 1]
     int32_t *list_len;      // [ticks + 1] list lengths, slot r

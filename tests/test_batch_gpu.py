@@ -61,6 +61,24 @@ def test_batch_scenarios_match_standalone(strategy, variant):
             assert np.array_equal(b.get_state(sid), want), "scenario %d" % sid
 
 
+@pytest.mark.parametrize("flavours", [(16, 0, 16), (0, 16, 4), (24, 5, 17)])
+def test_batch_count_flavours_switch_between_runs(flavours):
+    """Class bytes are kept by every count-strategy kernel and the activity bits
+    are rebuilt at the start of every run, so the class sweep can take over from
+    (or hand over to) the other count-step flavours between runs; every scenario
+    still equals its standalone run."""
+    scs = make_scenarios(16, 21, variant_lids=True)
+    with Batch() as b:
+        sids = [b.add_scenario(variant="B", **sc) for sc in scs]
+        b.commit()
+        for fl in flavours:
+            b.set_tune(strategy="count", count_flavour=fl)
+            b.run(25, use_graph=True)
+        b.synchronize()
+        for sid, sc in zip(sids, scs):
+            assert np.array_equal(b.get_state(sid), standalone(sc, "B", sc["horizon"])), "scenario %d" % sid
+
+
 def test_batch_matches_oracle_and_tuner_keeps_results():
     scs = make_scenarios(12, 9)
     with Batch() as b:

@@ -82,11 +82,15 @@ def test_sir_matches_oracle_every_tick(variant, strategy, kind):
             st = ref
 
 
-@pytest.mark.parametrize("flavour", range(8))
+COUNT_FLAVOURS = list(range(8)) + [8, 12, 16, 24, 31]
+
+
+@pytest.mark.parametrize("flavour", COUNT_FLAVOURS)
 @pytest.mark.parametrize("variant", ["A", "B"])
 def test_count_step_flavours_identical(flavour, variant):
     """Every count-step flavour (8 agents per thread, warp-dense draws, lazy
-    loads) gives the oracle's states; checked through the non-statistics path."""
+    loads, class sweep, either scatter) gives the oracle's states; checked
+    through the non-statistics path."""
     off, idx = hub_graph(5)
     n = off.size - 1
     st0 = _init_state(n, 0.01, 5)
@@ -102,3 +106,46 @@ def test_count_step_flavours_identical(flavour, variant):
         got = e.get_property(p)
     ref, _, _ = oracle.sir_run(1 if variant == "A" else 2, off, idx, st0, 9, 0, 45, 0.04, 0.08)
     assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("flavour", [0, 16])
+@pytest.mark.parametrize("variant", ["A", "B"])
+def test_count_dense_graph_with_statistics(flavour, variant):
+    """A dense graph with many infected neighbours per agent and a small beta
+    (long draw loops, every agent a candidate of the class sweep, activity bits
+    rebuilt after busy ticks): states and per-tick statistics match the oracle."""
+    off, idx = graphs.erdos_renyi(6000, 0.03, 2)
+    n = off.size - 1
+    st0 = _init_state(n, 0.4, 6)
+    beta, gamma = 0.005, 0.05
+    with Engine() as e:
+        e.set_graph(off, idx, symmetric=True)
+        e.set_seed(11)
+        p = e.add_property("state", np.int32, init=st0)
+        e.add_sir(p, beta, gamma, variant=variant, strategy="count")
+        e.set_tune(blocks_per_sm=8, count_flavour=flavour)
+        stats, _ = e.run(0, 12, stats=True)
+        got = e.get_property(p)
+    ref, rstats, _ = oracle.sir_run(1 if variant == "A" else 2, off, idx, st0, 11, 0, 12, beta, gamma)
+    assert np.array_equal(got, ref)
+    assert np.array_equal(stats, rstats)
+
+
+@pytest.mark.parametrize("variant", ["A", "B"])
+def test_class_sweep_statistics_on_power_law_graph(variant):
+    """Class sweep with statistics on a graph with hubs, through busy and quiet
+    ticks (bits kept by the scatter, then rebuilt, then kept again)."""
+    off, idx = hub_graph(7)
+    n = off.size - 1
+    st0 = _init_state(n, 0.002, 7)
+    with Engine() as e:
+        e.set_graph(off, idx, symmetric=True)
+        e.set_seed(5)
+        p = e.add_property("state", np.int32, init=st0)
+        e.add_sir(p, 0.2, 0.1, variant=variant, strategy="count")
+        e.set_tune(blocks_per_sm=16, count_flavour=16)
+        stats, _ = e.run(0, 60, stats=True)
+        got = e.get_property(p)
+    ref, rstats, _ = oracle.sir_run(1 if variant == "A" else 2, off, idx, st0, 5, 0, 60, 0.2, 0.1)
+    assert np.array_equal(got, ref)
+    assert np.array_equal(stats, rstats)
