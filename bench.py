@@ -287,8 +287,11 @@ def algorithmic_bytes(kernel, n, st0, tick_stats, active):
 
     sir_pull          12 B per agent (state read/write, row offset) + 4 B per CSR
                       entry of the tick-start susceptible agents (E_S)
-    sir_count_step    4 B state read per agent, 4 B count read per tick-start S
-                      agent, 8 B per transition (state write + change entry)
+    sir_count_step    class sweep (the default flavour): 1 B class read per agent,
+                      1/8 B activity bit per agent, 4 B RNG key per candidate
+                      (active[] = infected agents + susceptible agents with the
+                      bit set), 4 B count per susceptible candidate, 9 B per
+                      transition (state write, class write, change entry)
     frontier_step     20 B per active agent (list, state, count, mark, next list)
                       + 8 B per transition
     *_scatter         8 B per transition (change entry, transpose offsets) + 12 B
@@ -310,7 +313,9 @@ def algorithmic_bytes(kernel, n, st0, tick_stats, active):
     if kernel == "sir_pull":
         return 12.0 * n + 4.0 + 4.0 * E_S
     if kernel == "sir_count_step":
-        return 4.0 * n + 4.0 * S_start + 8.0 * changes
+        I = tick_stats[:, 1].astype(np.float64)
+        I_start = np.concatenate([[float((st0 == CODES[1]).sum())], I[:-1]])
+        return 1.125 * n + 4.0 * active + 4.0 * np.maximum(active - I_start, 0.0) + 9.0 * changes
     if kernel == "frontier_step":
         return 20.0 * active + 8.0 * changes
     if kernel in ("sir_count_scatter", "frontier_scatter"):

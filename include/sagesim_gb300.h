@@ -197,8 +197,10 @@ int sg_synchronize(sg_engine *e);
 int sg_engine_set_tune(sg_engine *e, const sg_tune *t);
 
 /* Agents the SIR step processed in each tick of the last sg_run/sg_run_async
- * (the active list length for the frontier strategy, the step's agent range
- * otherwise); n = number of ticks to report. Synchronizes the stream. */
+ * (the active list length for the frontier strategy; the candidates -- infected
+ * agents and susceptible agents whose activity bit is set -- for the class
+ * sweep; the step's agent range otherwise); n = number of ticks to report.
+ * Synchronizes the stream. */
 int sg_last_run_active(sg_engine *e, int64_t *out, int32_t n);
 
 /* Device snapshot of every property (checkpoint in HBM) and restore. */

@@ -403,9 +403,10 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickAr
 //      and four mask half-words per lane) and writes its candidates' slots to
 //      its part of shared memory;                                   -- barrier
 //   2. the block's threads share the concatenated candidate lists (U = 4 per
-//      thread in flight): count and RNG key, the draws (SIR-B: salt 2 .. 2+k-1
-//      in a per-thread loop with early exit), state, class and change-list
-//      writes (per-tile shared counters);                            -- barrier
+//      thread in flight): count and RNG key, the draws (recovery: salt 1;
+//      SIR-B infection: salt 2 .. 2+k-1 with early exit; one flattened loop
+//      over the thread's candidates), state, class and change-list writes
+//      (per-tile shared counters);                                   -- barrier
 //   3. each warp publishes its tile's change count and chunks.
 // Candidates cluster (an infected hub makes its whole neighbourhood, often a
 // few tiles, candidates at once); sharing a group's candidates among 8 warps
@@ -534,6 +535,7 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_sweep_kernel(SgTickA
         }
         if (lane == 0) {
             sh_ccount[warp] = C;
+            if (a.tick_cand && C > 0) atomicAdd(a.tick_cand + a.r, C);
             SgSweepTile tp = my;
             tp.live = (t < a.ntiles) && my.live;
             sh_tp[warp] = tp;
@@ -575,38 +577,75 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_sweep_kernel(SgTickA
                     ll[u] = lids ? __ldg(lids + i) : (uint32_t)(i - sh_tp[w].lid_base);
                 }
             }
+            // draws: one flattened loop over this thread's candidates (counter
+            // c0[u] + j, j < nd[u], until a hit), so a warp runs as long as its
+            // busiest thread's total draws rather than the sum of per-slot maxima
+            int32_t nd[U];
+            uint32_t c0[U], thr[U], kkey[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
+                nd[u] = 0;
+                c0[u] = thr[u] = kkey[u] = 0;
                 const int32_t i = gi[u];
                 if (i < 0) continue;
                 const SgSweepTile &tp = sh_tp[tw[u]];
-                bool hit = false;
+                kkey[u] = tp.key;
                 if (infk[u]) {
-                    hit = sg_philox_k23(tp.c0b + 1u, ll[u], tp.key) < tp.krec;
+                    nd[u] = 1;
+                    c0[u] = tp.c0b + 1u;
+                    thr[u] = tp.krec;
                 } else if (kk[u] > 0) {
-                    if (VARIANT == 1) {
-                        hit = sg_philox_k23(tp.c0b + 1u, ll[u], tp.key) < tp.kinf;
-                    } else {
-                        for (int32_t j = 0; j < kk[u]; ++j)
-                            if (sg_philox_k23(tp.c0b + 2u + (uint32_t)j, ll[u], tp.key) < tp.kinf) {
-                                hit = true;
-                                break;
-                            }
-                    }
+                    nd[u] = VARIANT == 1 ? 1 : kk[u];
+                    c0[u] = tp.c0b + (VARIANT == 1 ? 1u : 2u);
+                    thr[u] = tp.kinf;
                 } else {
                     atomicAnd(a.amask + (i >> 5), ~(1u << (i & 31)));
                 }
-                if (hit) {
-                    state[i] = infk[u] ? tp.cr : tp.ci;
-                    a.cls[i] = (uint8_t)(infk[u] ? 2 : 1);
-                    const int32_t p = atomicAdd(&sh_nch[tw[u]], 1);
-                    a.changes[tp.begin + p] = infk[u] ? ~i : i;
-                    if (a.rowsegs) publish_long_row(a, i, infk[u] ? -1 : 1);
-                    if (STATS) {
-                        // S -> I: S - 1, I + 1; I -> R: I - 1, R + 1 (sums mod 2^64)
-                        atomicAdd(&sh_dstat[tw[u]][infk[u] ? 1 : 0], ~0ull);
-                        atomicAdd(&sh_dstat[tw[u]][infk[u] ? 2 : 1], 1ull);
+            }
+            uint32_t hitm = 0;
+            int cur = -1;
+            int32_t left = 0;
+            uint32_t cc = 0, cl = 0, ct = 0, ckey = 0;
+            auto next = [&](int from) {
+                cur = -1;
+#pragma unroll
+                for (int v = U - 1; v >= 0; --v)
+                    if (v >= from && nd[v] > 0) cur = v;
+#pragma unroll
+                for (int v = 0; v < U; ++v)
+                    if (v == cur) {
+                        left = nd[v];
+                        cc = c0[v];
+                        cl = ll[v];
+                        ct = thr[v];
+                        ckey = kkey[v];
                     }
+            };
+            next(0);
+            while (cur >= 0) {
+                const bool h = sg_philox_k23(cc, cl, ckey) < ct;
+                ++cc;
+                if (h) {
+                    hitm |= 1u << cur;
+                    next(cur + 1);
+                } else if (--left == 0) {
+                    next(cur + 1);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (!((hitm >> u) & 1u)) continue;
+                const int32_t i = gi[u];
+                const SgSweepTile &tp = sh_tp[tw[u]];
+                state[i] = infk[u] ? tp.cr : tp.ci;
+                a.cls[i] = (uint8_t)(infk[u] ? 2 : 1);
+                const int32_t p = atomicAdd(&sh_nch[tw[u]], 1);
+                a.changes[tp.begin + p] = infk[u] ? ~i : i;
+                if (a.rowsegs) publish_long_row(a, i, infk[u] ? -1 : 1);
+                if (STATS) {
+                    // S -> I: S - 1, I + 1; I -> R: I - 1, R + 1 (sums mod 2^64)
+                    atomicAdd(&sh_dstat[tw[u]][infk[u] ? 1 : 0], ~0ull);
+                    atomicAdd(&sh_dstat[tw[u]][infk[u] ? 2 : 1], 1ull);
                 }
             }
         }

@@ -75,8 +75,9 @@ struct sg_engine {
 
     // scratch of the count strategy and of per-tick statistics
     SgDev cnt, changes, tile_nch, stats, chunks, nchunks, rowsegs, nrowsegs;
-    SgDev cls, amask, mrebuild, tick_changes; // class sweep: classes, activity bits, per-tick flags
-    bool cls_on = false; // this run's count step keeps classes (its tiles start at multiples of 32)
+    SgDev cls, amask, mrebuild, tick_changes, tick_cand; // class sweep: classes, activity bits, per-tick counters
+    bool cls_on = false;     // this run's count step keeps classes (its tiles start at multiples of 32)
+    bool last_sweep = false; // the last run's count step was the class sweep
     SgDev flist[2], flen, fnch, fmark, fstats_init, fstats_delta; // frontier strategy
     SgDev transpose_tmp, scan_tmp;
     SgDev prop_table; // sg_prop_dev per property, for compiled steps
@@ -581,6 +582,7 @@ static SgTickArgs base_args(sg_engine *e, SgStep *s, int32_t r, bool inplace)
         a.amask = e->amask.as<uint32_t>();
         a.mrebuild = e->mrebuild.as<uint8_t>();
         a.tick_changes = e->tick_changes.as<int32_t>();
+        a.tick_cand = e->tick_cand.as<int32_t>();
     }
     const bool sym = (e->graph_flags & SG_GRAPH_SYMMETRIC) != 0;
     a.toff = sym ? e->off.as<int32_t>() : e->toff.as<int32_t>();
@@ -646,6 +648,7 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
         if (e->cls_on) { // the init builds exact activity bits: no rebuild at r == 0
             SG_CK(cudaMemsetAsync(e->mrebuild.p, 0, (size_t)nticks + 1, e->stream));
             SG_CK(cudaMemsetAsync(e->tick_changes.p, 0, (size_t)std::max(nticks, 1) * 4, e->stream));
+            SG_CK(cudaMemsetAsync(e->tick_cand.p, 0, (size_t)std::max(nticks, 1) * 4, e->stream));
         }
         SG_PROF_LAUNCH("sir_count_init",
                        sg_launch_sir_count_init(a, grid_for(e, s->ntiles) + a.mega_blocks, e->stream));
@@ -765,7 +768,9 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
         SG_CK(e->amask.reserve(((size_t)e->n / 32 + 2) * 4));
         SG_CK(e->mrebuild.reserve((size_t)nticks + 1));
         SG_CK(e->tick_changes.reserve((size_t)std::max(nticks, 1) * 4));
+        SG_CK(e->tick_cand.reserve((size_t)std::max(nticks, 1) * 4));
     }
+    e->last_sweep = e->cls_on && pl.count_inplace && (e->tune.count_flavour & SG_FLAVOUR_SWEEP);
     return SG_OK;
 }
 
@@ -910,6 +915,13 @@ int sg_last_run_active(sg_engine *e, int64_t *out, int32_t n)
         std::vector<int32_t> len((size_t)n);
         if (n) SG_CK(cudaMemcpy(len.data(), e->flen.p, (size_t)n * 4, cudaMemcpyDeviceToHost));
         for (int32_t r = 0; r < n; ++r) out[r] = len[(size_t)r];
+        return SG_OK;
+    }
+    if (e->last_sweep) { // candidates of the class sweep
+        if (n > e->last_nticks) return e->fail(SG_ERR_INVALID, "n exceeds the last run's ticks");
+        std::vector<int32_t> c((size_t)n);
+        if (n) SG_CK(cudaMemcpy(c.data(), e->tick_cand.p, (size_t)n * 4, cudaMemcpyDeviceToHost));
+        for (int32_t r = 0; r < n; ++r) out[r] = c[(size_t)r];
         return SG_OK;
     }
     int64_t agents = 0;

@@ -96,6 +96,8 @@ struct SgTickArgs {
                             // them from the counts; zero before the run
     int32_t *tick_changes;  // with mrebuild: [ticks] changes recorded by the sweep at
                             // tick r (zero before the run)
+    int32_t *tick_cand;     // NULL, or [ticks] candidates the sweep processed at tick r
+                            // (zero before the run)
     // frontier strategy
     int32_t *list[2];       // active agents of tick r in list[r & 1]
     int32_t *list_len;      // [ticks + 1] list lengths, slot r
