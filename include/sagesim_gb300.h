@@ -133,7 +133,9 @@ typedef struct sg_tune {
                                /*  2 = warp-dense SIR-B draws                    */
                                /*  4 = count and RNG key loaded only where needed*/
                                /*  8 = scatter: one transpose row per lane       */
-                               /* 16 = class sweep (in-place runs)               */
+                               /* 16 = class sweep (in-place runs, graphs of at  */
+                               /*      least 8 tiles of 2048 agents per SM)      */
+                               /* 32 = class sweep on graphs of any size         */
     double us_per_tick;        /* measured by sg_batch_tune (output)             */
 } sg_tune;
 

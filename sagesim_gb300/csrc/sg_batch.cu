@@ -27,8 +27,8 @@ constexpr int32_t kLongRowFloor = 512; // rows kept as mega candidates (smallest
 // count-step flavours the autotuner times: loop form (4 or 8 agents per thread,
 // eager or lazy loads) and class sweep with the load-balanced scatter, and two
 // of them with the lane-per-row scatter
-constexpr int32_t kCountFlavourCands[] = {0, 1, 4, 5, SG_FLAVOUR_SWEEP, SG_FLAVOUR_ROWSCATTER | 4,
-                                          SG_FLAVOUR_ROWSCATTER | SG_FLAVOUR_SWEEP};
+constexpr int32_t kCountFlavourCands[] = {0, 1, 4, 5, SG_FLAVOUR_SWEEP, SG_FLAVOUR_SWEEP | SG_FLAVOUR_FORCE,
+                                          SG_FLAVOUR_ROWSCATTER | 4, SG_FLAVOUR_ROWSCATTER | SG_FLAVOUR_SWEEP};
 }
 
 int64_t SgRanges::take(int64_t len)
@@ -307,6 +307,9 @@ int SgPool::enqueue(int32_t nticks, bool capturing)
     a.ntiles = (int32_t)htiles.size();
     a.thread_row = tune.thread_row;
     a.flavour = tune.count_flavour;
+    if ((a.flavour & SG_FLAVOUR_SWEEP) && !(a.flavour & SG_FLAVOUR_FORCE) &&
+        (int64_t)htiles.size() < (int64_t)sm_count * SG_SWEEP_MIN_TILES_PER_SM)
+        a.flavour = (a.flavour & ~SG_FLAVOUR_SWEEP) | SG_FLAVOUR_LAZY;
     a.mega = mega.as<SgMega>();
     a.nmega = (int32_t)hmega.size();
     a.mega_blocks = std::min<int32_t>(a.nmega, sm_count);

@@ -398,7 +398,8 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickAr
 // epidemic a tick reads about one byte per agent instead of its state, count
 // and RNG key.
 //
-// A block takes a group of 8 consecutive tiles, one warp per tile:
+// A block takes a group of 8 tiles, one warp per tile (group g: tiles g,
+// g + G, g + 2G, ... with G groups):
 //   1. each warp reads its tile's classes and bits (four 16-byte class loads
 //      and four mask half-words per lane) and writes its candidates' slots to
 //      its part of shared memory;                                   -- barrier
@@ -409,9 +410,10 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickAr
 //      (per-tile shared counters);                                   -- barrier
 //   3. each warp publishes its tile's change count and chunks.
 // Candidates cluster (an infected hub makes its whole neighbourhood, often a
-// few tiles, candidates at once); sharing a group's candidates among 8 warps
-// keeps such tiles from serialising on one warp, and a group costs three
-// dependent memory round trips and two barriers. A count read as 0 clears its
+// few consecutive tiles, candidates at once); spreading consecutive tiles over
+// blocks and sharing a group's candidates among its 8 warps keeps such tiles
+// from serialising on one warp or block, and a group costs three dependent
+// memory round trips and two barriers. A count read as 0 clears its
 // bit. In a rebuild tick (the previous scatter did not keep the bits) every
 // susceptible agent is a candidate: phase 1 sets the bits of all of them and
 // phase 2 clears those whose count is 0.
@@ -444,7 +446,9 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_sweep_kernel(SgTickA
     if (tid < kWarps) sh_nch[tid] = 0;
     for (int32_t g = blockIdx.x; g < ngroups; g += gridDim.x) {
         // 1. this warp's tile: classes and bits -> candidate list
-        const int32_t t = g * kWarps + warp;
+        // tiles of a group are ngroups apart, so a cluster of candidate-dense
+        // consecutive tiles (a hub's neighbourhood) is spread over 8 blocks
+        const int32_t t = warp * ngroups + g;
         int32_t C = 0;
         unsigned long long nS = 0, nI = 0, nR = 0, eS = 0;
         if (t < a.ntiles) {

@@ -565,6 +565,9 @@ static SgTickArgs base_args(sg_engine *e, SgStep *s, int32_t r, bool inplace)
     a.r = r;
     a.thread_row = e->tune.thread_row;
     a.flavour = e->tune.count_flavour;
+    if ((a.flavour & SG_FLAVOUR_SWEEP) && !(a.flavour & SG_FLAVOUR_FORCE) &&
+        s->ntiles < e->sm_count * SG_SWEEP_MIN_TILES_PER_SM)
+        a.flavour = (a.flavour & ~SG_FLAVOUR_SWEEP) | SG_FLAVOUR_LAZY;
     a.mega = s->mega.as<SgMega>();
     a.nmega = s->nmega;
     a.mega_blocks = std::min(s->nmega, e->sm_count);
@@ -770,7 +773,9 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
         SG_CK(e->tick_changes.reserve((size_t)std::max(nticks, 1) * 4));
         SG_CK(e->tick_cand.reserve((size_t)std::max(nticks, 1) * 4));
     }
-    e->last_sweep = e->cls_on && pl.count_inplace && (e->tune.count_flavour & SG_FLAVOUR_SWEEP);
+    e->last_sweep = e->cls_on && pl.count_inplace && (e->tune.count_flavour & SG_FLAVOUR_SWEEP) &&
+                    ((e->tune.count_flavour & SG_FLAVOUR_FORCE) ||
+                     pl.count_step->ntiles >= e->sm_count * SG_SWEEP_MIN_TILES_PER_SM);
     return SG_OK;
 }
 

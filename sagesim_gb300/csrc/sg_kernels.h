@@ -46,7 +46,12 @@ struct SgMega {
 #define SG_FLAVOUR_ROWSCATTER 8 // scatter walks one transpose row per lane instead of
                                 // the warp's rows laid end to end
 #define SG_FLAVOUR_SWEEP 16 // class sweep (in-place runs that keep class bytes)
-#define SG_FLAVOUR_MAX 31
+#define SG_FLAVOUR_FORCE 32 // class sweep on any graph size (see below)
+// The class sweep runs one warp per tile; below this many tiles per SM it
+// leaves SMs idle and the loop form (lazy loads) is used instead, unless
+// SG_FLAVOUR_FORCE is set.
+#define SG_SWEEP_MIN_TILES_PER_SM 8
+#define SG_FLAVOUR_MAX 63
 
 // One warp's share of the scatter: changes [32 * chunk, 32 * chunk + 32) of a tile.
 struct SgChunk {
