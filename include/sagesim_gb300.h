@@ -134,8 +134,10 @@ typedef struct sg_tune {
                                /*  4 = count and RNG key loaded only where needed*/
                                /*  8 = scatter: one transpose row per lane       */
                                /* 16 = class sweep (in-place runs, graphs of at  */
-                               /*      least 8 tiles of 2048 agents per SM)      */
+                               /*      least 2 tiles of 2048 agents per SM)      */
                                /* 32 = class sweep on graphs of any size         */
+                               /* bits 6-7: sweep warps per tile, 0 = automatic, */
+                               /*      1/2/3 = 1/2/4 warps                       */
     double us_per_tick;        /* measured by sg_batch_tune (output)             */
 } sg_tune;
 

@@ -425,30 +425,34 @@ struct SgSweepTile {
     unsigned long long *stats;
 };
 
-template <int VARIANT, bool STATS>
+template <int VARIANT, bool STATS, int WPT>
 __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_sweep_kernel(SgTickArgs a)
 {
     constexpr int kRun = 16;                     // agents per lane and class load
-    constexpr int kRuns = SG_TILE / (32 * kRun); // runs of a lane in a tile
+    constexpr int kRuns = SG_TILE / (32 * kRun); // runs of a whole tile per lane
+    constexpr int kMyRuns = kRuns / WPT;         // runs of this warp's part of a tile
+    constexpr int TPB = kWarps / WPT;            // tiles per block (group)
     constexpr int U = 4;                         // candidates per thread in flight
     static_assert(kRuns * 32 * kRun == SG_TILE, "runs must cover the tile");
+    static_assert(kMyRuns * WPT == kRuns && TPB * WPT == kWarps, "warps must split tiles evenly");
     static_assert(SG_TILE <= 0x800, "slot must fit in 11 bits");
     __shared__ uint16_t sh_cand[kWarps][SG_TILE]; // slot | infected << 11
     __shared__ SgSweepTile sh_tp[kWarps];
-    __shared__ int32_t sh_ccount[kWarps], sh_nch[kWarps];
-    __shared__ unsigned long long sh_dstat[kWarps][3]; // per tile: S, I, R changes (mod 2^64)
+    __shared__ int32_t sh_ccount[kWarps], sh_nch[TPB];
+    __shared__ unsigned long long sh_dstat[kWarps][3]; // per warp region: S, I, R changes (mod 2^64)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ti = warp / WPT, part = warp % WPT; // this warp's tile in the group and part of it
     int32_t *const state = (int32_t *)a.buf0;
     const bool rebuild = a.mrebuild && a.mrebuild[a.r];
-    const int32_t ngroups = (a.ntiles + kWarps - 1) / kWarps;
+    const int32_t ngroups = (a.ntiles + TPB - 1) / TPB;
     int32_t cur_seg = -1; // this warp's cached segment
     SgSweepTile my{};
-    if (tid < kWarps) sh_nch[tid] = 0;
+    if (tid < TPB) sh_nch[tid] = 0;
     for (int32_t g = blockIdx.x; g < ngroups; g += gridDim.x) {
-        // 1. this warp's tile: classes and bits -> candidate list
+        // 1. this warp's part of its tile: classes and bits -> candidate list
         // tiles of a group are ngroups apart, so a cluster of candidate-dense
-        // consecutive tiles (a hub's neighbourhood) is spread over 8 blocks
-        const int32_t t = warp * ngroups + g;
+        // consecutive tiles (a hub's neighbourhood) is spread over TPB blocks
+        const int32_t t = ti * ngroups + g;
         int32_t C = 0;
         unsigned long long nS = 0, nI = 0, nR = 0, eS = 0;
         if (t < a.ntiles) {
@@ -471,9 +475,10 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_sweep_kernel(SgTickA
             my.begin = tile.begin;
             if (my.live) {
                 uint16_t *const wcand = sh_cand[warp];
-                uint32_t cm[kRuns], im[kRuns];
+                uint32_t cm[kMyRuns], im[kMyRuns];
 #pragma unroll
-                for (int r = 0; r < kRuns; ++r) {
+                for (int rr = 0; rr < kMyRuns; ++rr) {
+                    const int r = part * kMyRuns + rr;
                     const int32_t b = tile.begin + r * (32 * kRun) + lane * kRun;
                     const int32_t nv = min(kRun, tile.end - b);
                     uint32_t w[4] = {0x03030303u, 0x03030303u, 0x03030303u, 0x03030303u};
@@ -506,8 +511,8 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_sweep_kernel(SgTickA
                         word |= __shfl_xor_sync(FULL_MASK, word, 1);
                         if (!(lane & 1) && nv > 0) a.amask[b >> 5] = word;
                     }
-                    cm[r] = (rebuild ? sm : (sm & bits)) | imr;
-                    im[r] = imr;
+                    cm[rr] = (rebuild ? sm : (sm & bits)) | imr;
+                    im[rr] = imr;
                     if (STATS) {
                         nS += __popc(sm);
                         nI += __popc(imr);
@@ -520,7 +525,7 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_sweep_kernel(SgTickA
                 }
                 int32_t mine = 0;
 #pragma unroll
-                for (int r = 0; r < kRuns; ++r) mine += __popc(cm[r]);
+                for (int rr = 0; rr < kMyRuns; ++rr) mine += __popc(cm[rr]);
                 int32_t x = mine;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
@@ -530,10 +535,11 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_sweep_kernel(SgTickA
                 C = __shfl_sync(FULL_MASK, x, 31);
                 int32_t pos = x - mine;
 #pragma unroll
-                for (int r = 0; r < kRuns; ++r)
-                    for (uint32_t m = cm[r]; m; m &= m - 1) {
+                for (int rr = 0; rr < kMyRuns; ++rr)
+                    for (uint32_t m = cm[rr]; m; m &= m - 1) {
                         const int e = __ffs(m) - 1;
-                        wcand[pos++] = (uint16_t)((r * (32 * kRun) + lane * kRun + e) | (((im[r] >> e) & 1u) << 11));
+                        const int r = part * kMyRuns + rr;
+                        wcand[pos++] = (uint16_t)((r * (32 * kRun) + lane * kRun + e) | (((im[rr] >> e) & 1u) << 11));
                     }
             }
         }
@@ -643,7 +649,7 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_sweep_kernel(SgTickA
                 const SgSweepTile &tp = sh_tp[tw[u]];
                 state[i] = infk[u] ? tp.cr : tp.ci;
                 a.cls[i] = (uint8_t)(infk[u] ? 2 : 1);
-                const int32_t p = atomicAdd(&sh_nch[tw[u]], 1);
+                const int32_t p = atomicAdd(&sh_nch[tw[u] / WPT], 1);
                 a.changes[tp.begin + p] = infk[u] ? ~i : i;
                 if (a.rowsegs) publish_long_row(a, i, infk[u] ? -1 : 1);
                 if (STATS) {
@@ -654,9 +660,9 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_sweep_kernel(SgTickA
             }
         }
         __syncthreads();
-        // 3. this warp's tile: change count, chunks, statistics
-        if (t < a.ntiles) {
-            const int32_t n = sh_nch[warp];
+        // 3. the tile's change count and chunks (its first warp), statistics (every warp)
+        if (t < a.ntiles && part == 0) {
+            const int32_t n = sh_nch[ti];
             if (lane == 0) {
                 a.tile_nch[t] = n;
                 if (a.tick_changes && n > 0) atomicAdd(a.tick_changes + a.r, n);
@@ -668,6 +674,8 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_sweep_kernel(SgTickA
                 cb = __shfl_sync(FULL_MASK, cb, 0);
                 for (int32_t j = lane; j < c; j += 32) a.chunks[cb + j] = SgChunk{t, j};
             }
+        }
+        if (t < a.ntiles) {
             if (STATS && my.live && my.stats) {
                 const unsigned long long v0 = warp_sum(nS), v1 = warp_sum(nI), v2 = warp_sum(nR),
                                          v3 = warp_sum(eS);
@@ -681,7 +689,7 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_sweep_kernel(SgTickA
             }
         }
         __syncwarp();
-        if (lane == 0) sh_nch[warp] = 0; // read above by this warp only
+        if (lane == 0 && part == 0) sh_nch[ti] = 0; // read above by this warp only
     }
 }
 
@@ -888,14 +896,18 @@ cudaError_t sg_launch_sir_count_step(const SgTickArgs &a, int variant, bool stat
                                      int grid, cudaStream_t st)
 {
     if ((a.flavour & SG_FLAVOUR_SWEEP) && inplace && a.cls && a.chunks) {
-        grid = std::max(1, std::min(grid, (a.ntiles + kWarps - 1) / kWarps)); // a group of 8 tiles per block
+        const int wpt = a.sweep_wpt == 2 || a.sweep_wpt == 4 ? a.sweep_wpt : 1;
+        const int tpb = kWarps / wpt;
+        grid = std::max(1, std::min(grid, (a.ntiles + tpb - 1) / tpb)); // one group of tpb tiles per block
+#define SG_SW(V, S, W) sir_count_sweep_kernel<V, S, W><<<grid, SG_SIR_THREADS, 0, st>>>(a)
+#define SG_SWW(V, S) (wpt == 1 ? SG_SW(V, S, 1) : wpt == 2 ? SG_SW(V, S, 2) : SG_SW(V, S, 4))
         if (variant == 1) {
-            if (stats) sir_count_sweep_kernel<1, true><<<grid, SG_SIR_THREADS, 0, st>>>(a);
-            else sir_count_sweep_kernel<1, false><<<grid, SG_SIR_THREADS, 0, st>>>(a);
+            if (stats) SG_SWW(1, true); else SG_SWW(1, false);
         } else {
-            if (stats) sir_count_sweep_kernel<2, true><<<grid, SG_SIR_THREADS, 0, st>>>(a);
-            else sir_count_sweep_kernel<2, false><<<grid, SG_SIR_THREADS, 0, st>>>(a);
+            if (stats) SG_SWW(2, true); else SG_SWW(2, false);
         }
+#undef SG_SWW
+#undef SG_SW
         return cudaGetLastError();
     }
     if (stats) { // statistics runs of the loop form use one flavour

@@ -47,11 +47,26 @@ struct SgMega {
                                 // the warp's rows laid end to end
 #define SG_FLAVOUR_SWEEP 16 // class sweep (in-place runs that keep class bytes)
 #define SG_FLAVOUR_FORCE 32 // class sweep on any graph size (see below)
+#define SG_FLAVOUR_WPT_SHIFT 6 // bits 6-7: class-sweep warps per tile, 0 = automatic
+                              // (sg_sweep_wpt), 1/2/3 = 1/2/4 warps
+#define SG_FLAVOUR_MAX 255
 // The class sweep runs one warp per tile; below this many tiles per SM it
 // leaves SMs idle and the loop form (lazy loads) is used instead, unless
 // SG_FLAVOUR_FORCE is set.
-#define SG_SWEEP_MIN_TILES_PER_SM 8
-#define SG_FLAVOUR_MAX 63
+#define SG_SWEEP_MIN_TILES_PER_SM 2
+
+// Warps per tile of the class sweep: one warp per tile while there are enough
+// tiles to give every SM its 4 resident blocks of 8 warps, else 2 or 4 warps
+// share a tile so that smaller graphs still fill the SMs.
+inline int32_t sg_sweep_wpt(int64_t ntiles, int sm_count, int32_t flavour)
+{
+    const int32_t forced = (flavour >> SG_FLAVOUR_WPT_SHIFT) & 3;
+    if (forced) return 1 << (forced - 1);
+    const int64_t resident = (int64_t)sm_count * 4;
+    if (ntiles >= 8 * resident) return 1;
+    if (ntiles >= 4 * resident) return 2;
+    return 4;
+}
 
 // One warp's share of the scatter: changes [32 * chunk, 32 * chunk + 32) of a tile.
 struct SgChunk {
@@ -103,6 +118,7 @@ struct SgTickArgs {
                             // tick r (zero before the run)
     int32_t *tick_cand;     // NULL, or [ticks] candidates the sweep processed at tick r
                             // (zero before the run)
+    int32_t sweep_wpt;      // class sweep: warps per tile (1, 2 or 4; see sg_sweep_wpt)
     // frontier strategy
     int32_t *list[2];       // active agents of tick r in list[r & 1]
     int32_t *list_len;      // [ticks + 1] list lengths, slot r

@@ -82,7 +82,7 @@ def test_sir_matches_oracle_every_tick(variant, strategy, kind):
             st = ref
 
 
-COUNT_FLAVOURS = list(range(8)) + [8, 12, 16, 24, 48, 56, 63]
+COUNT_FLAVOURS = list(range(8)) + [8, 12, 16, 24, 48, 56, 63, 48 | 64, 48 | 128, 56 | 192]
 
 
 @pytest.mark.parametrize("flavour", COUNT_FLAVOURS)
@@ -108,7 +108,7 @@ def test_count_step_flavours_identical(flavour, variant):
     assert np.array_equal(got, ref)
 
 
-@pytest.mark.parametrize("flavour", [0, 16, 48])
+@pytest.mark.parametrize("flavour", [0, 16, 48, 48 | 64, 48 | 128])
 @pytest.mark.parametrize("variant", ["A", "B"])
 def test_count_dense_graph_with_statistics(flavour, variant):
     """A dense graph with many infected neighbours per agent and a small beta
@@ -131,8 +131,9 @@ def test_count_dense_graph_with_statistics(flavour, variant):
     assert np.array_equal(stats, rstats)
 
 
+@pytest.mark.parametrize("wpt_bits", [64, 128, 192])
 @pytest.mark.parametrize("variant", ["A", "B"])
-def test_class_sweep_statistics_on_power_law_graph(variant):
+def test_class_sweep_statistics_on_power_law_graph(variant, wpt_bits):
     """Class sweep with statistics on a graph with hubs, through busy and quiet
     ticks (bits kept by the scatter, then rebuilt, then kept again)."""
     off, idx = hub_graph(7)
@@ -143,7 +144,7 @@ def test_class_sweep_statistics_on_power_law_graph(variant):
         e.set_seed(5)
         p = e.add_property("state", np.int32, init=st0)
         e.add_sir(p, 0.2, 0.1, variant=variant, strategy="count")
-        e.set_tune(blocks_per_sm=16, count_flavour=48)
+        e.set_tune(blocks_per_sm=16, count_flavour=48 | wpt_bits)
         stats, _ = e.run(0, 60, stats=True)
         got = e.get_property(p)
     ref, rstats, _ = oracle.sir_run(1 if variant == "A" else 2, off, idx, st0, 5, 0, 60, 0.2, 0.1)
