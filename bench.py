@@ -287,11 +287,14 @@ def algorithmic_bytes(kernel, n, st0, tick_stats, active):
 
     sir_pull          12 B per agent (state read/write, row offset) + 4 B per CSR
                       entry of the tick-start susceptible agents (E_S)
-    sir_count_step    class sweep (the default flavour): 1 B class read per agent,
+    sir_count_step    class sweep ticks: 1 B class read per agent,
                       1/8 B activity bit per agent, 4 B RNG key per candidate
                       (active[] = infected agents + susceptible agents with the
                       bit set), 4 B count per susceptible candidate, 9 B per
-                      transition (state write, class write, change entry)
+                      transition (state write, class write, change entry);
+                      loop-form ticks (hybrid step in busy ticks): 4 B state read
+                      per agent, 4 B count read per tick-start S agent, 8 B per
+                      transition
     frontier_step     20 B per active agent (list, state, count, mark, next list)
                       + 8 B per transition
     *_scatter         8 B per transition (change entry, transpose offsets) + 12 B
@@ -313,9 +316,12 @@ def algorithmic_bytes(kernel, n, st0, tick_stats, active):
     if kernel == "sir_pull":
         return 12.0 * n + 4.0 + 4.0 * E_S
     if kernel == "sir_count_step":
+        # ticks the hybrid step gave to the loop form report every agent as processed
         I = tick_stats[:, 1].astype(np.float64)
         I_start = np.concatenate([[float((st0 == CODES[1]).sum())], I[:-1]])
-        return 1.125 * n + 4.0 * active + 4.0 * np.maximum(active - I_start, 0.0) + 9.0 * changes
+        sweep = 1.125 * n + 4.0 * active + 4.0 * np.maximum(active - I_start, 0.0) + 9.0 * changes
+        loop = 4.0 * n + 4.0 * S_start + 8.0 * changes
+        return np.where(active >= n, loop, sweep)
     if kernel == "frontier_step":
         return 20.0 * active + 8.0 * changes
     if kernel in ("sir_count_scatter", "frontier_scatter"):
@@ -409,7 +415,7 @@ def sweep(args):
         eng.snapshot()
         ref = None
         for bps in (8, 16):
-            for fl in (0, 1, 4, 5, 8, 12, 16, 24):
+            for fl in (0, 4, 5, 16, 24, 16 | 256 | 4, 16 | 256 | 5, 16 | 256):
                 eng.set_tune(blocks_per_sm=bps, count_flavour=fl)
                 for _ in range(2):
                     eng.restore()

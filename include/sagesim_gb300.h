@@ -138,6 +138,8 @@ typedef struct sg_tune {
                                /* 32 = class sweep on graphs of any size         */
                                /* bits 6-7: sweep warps per tile, 0 = automatic, */
                                /*      1/2/3 = 1/2/4 warps                       */
+                               /* 256 = with 16: hybrid, the loop form of bits   */
+                               /*      0-2 in busy ticks (decided on the GPU)    */
     double us_per_tick;        /* measured by sg_batch_tune (output)             */
 } sg_tune;
 

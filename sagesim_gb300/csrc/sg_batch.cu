@@ -308,6 +308,7 @@ int SgPool::enqueue(int32_t nticks, bool capturing)
     a.thread_row = tune.thread_row;
     a.flavour = tune.count_flavour;
     a.sweep_wpt = sg_sweep_wpt((int64_t)htiles.size(), sm_count, a.flavour);
+    sg_hybrid_thresholds((int64_t)htiles.size(), a.flavour, &a.hybrid_rise, &a.hybrid_fall);
     if ((a.flavour & SG_FLAVOUR_SWEEP) && !(a.flavour & SG_FLAVOUR_FORCE) &&
         (int64_t)htiles.size() < (int64_t)sm_count * SG_SWEEP_MIN_TILES_PER_SM)
         a.flavour = (a.flavour & ~SG_FLAVOUR_SWEEP) | SG_FLAVOUR_LAZY;

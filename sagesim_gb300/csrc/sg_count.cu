@@ -165,6 +165,20 @@ __device__ __forceinline__ unsigned warp_dense_sirb(const int32_t (&k)[P], const
     return bits;
 }
 
+// Hybrid count step. Both step kernels are launched each tick; the one not
+// chosen returns at once. The choice reads the change totals of the two
+// previous ticks, which every block of both kernels sees alike. The loop form
+// pays a fixed cost per agent, the class sweep one per candidate; while an
+// epidemic grows, candidates (susceptible agents next to new infections, often
+// clustered around hubs) outnumber changes by far, so the loop form is chosen
+// from a lower change count on the way up than on the way down.
+__device__ __forceinline__ bool hybrid_loop_tick(const SgTickArgs &a)
+{
+    if (a.hybrid_rise <= 0 || a.r < 2 || !a.tick_changes) return false;
+    const int32_t c1 = a.tick_changes[a.r - 1], c2 = a.tick_changes[a.r - 2];
+    return (c1 > a.hybrid_rise && c1 >= c2) || c1 > a.hybrid_fall;
+}
+
 // A changed agent whose transpose row is longer than kSegRow is handed to the
 // scatter as row segments of kSegRow entries on their own work list, so no
 // single warp walks a hub's whole row; the chunk pass skips such rows.
@@ -196,6 +210,11 @@ template <int VARIANT, bool STATS, bool INPLACE, int PER, bool DENSE, bool LAZY>
 __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickArgs a)
 {
     static_assert(SG_TILE % (SG_SIR_THREADS * PER) == 0, "tile must be whole passes");
+    if (a.hybrid_rise > 0) {
+        if (!hybrid_loop_tick(a)) return; // the class sweep takes this tick
+        // activity bits owed a rebuild stay owed until a sweep tick rebuilds them
+        if (blockIdx.x == 0 && threadIdx.x == 0 && a.mrebuild && a.mrebuild[a.r]) a.mrebuild[a.r + 1] = 1;
+    }
     __shared__ unsigned long long red[4][kWarps];
     __shared__ int32_t nch, chunk_base;
     __shared__ unsigned char wflags[DENSE ? SG_SIR_THREADS * PER : 1];
@@ -375,6 +394,8 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickAr
             const int32_t c = (n + 31) >> 5;
             if (tid == 0) {
                 a.tile_nch[t] = n;
+                if (a.tick_changes && n > 0) atomicAdd(a.tick_changes + a.r, n);
+                if (a.tick_cand) atomicAdd(a.tick_cand + a.r, tile.end - tile.begin);
                 if (a.chunks && n > 0) chunk_base = atomicAdd(a.nchunks + a.r, c);
             }
             __syncthreads();
@@ -440,6 +461,7 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_sweep_kernel(SgTickA
     __shared__ SgSweepTile sh_tp[kWarps];
     __shared__ int32_t sh_ccount[kWarps], sh_nch[TPB];
     __shared__ unsigned long long sh_dstat[kWarps][3]; // per warp region: S, I, R changes (mod 2^64)
+    if (hybrid_loop_tick(a)) return; // the loop form takes this tick
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int ti = warp / WPT, part = warp % WPT; // this warp's tile in the group and part of it
     int32_t *const state = (int32_t *)a.buf0;
@@ -892,14 +914,17 @@ static void count_step_flavour(const SgTickArgs &a, int flavour, int grid, cudaS
 #undef SG_CF
 }
 
-cudaError_t sg_launch_sir_count_step(const SgTickArgs &a, int variant, bool stats, bool inplace,
+cudaError_t sg_launch_sir_count_step(const SgTickArgs &args, int variant, bool stats, bool inplace,
                                      int grid, cudaStream_t st)
 {
-    if ((a.flavour & SG_FLAVOUR_SWEEP) && inplace && a.cls && a.chunks) {
+    SgTickArgs a = args;
+    const bool sweep = (a.flavour & SG_FLAVOUR_SWEEP) && inplace && a.cls && a.chunks;
+    if (!sweep) a.hybrid_rise = 0; // the loop form takes every tick
+    if (sweep) {
         const int wpt = a.sweep_wpt == 2 || a.sweep_wpt == 4 ? a.sweep_wpt : 1;
         const int tpb = kWarps / wpt;
-        grid = std::max(1, std::min(grid, (a.ntiles + tpb - 1) / tpb)); // one group of tpb tiles per block
-#define SG_SW(V, S, W) sir_count_sweep_kernel<V, S, W><<<grid, SG_SIR_THREADS, 0, st>>>(a)
+        const int sgrid = std::max(1, std::min(grid, (a.ntiles + tpb - 1) / tpb)); // one group of tpb tiles per block
+#define SG_SW(V, S, W) sir_count_sweep_kernel<V, S, W><<<sgrid, SG_SIR_THREADS, 0, st>>>(a)
 #define SG_SWW(V, S) (wpt == 1 ? SG_SW(V, S, 1) : wpt == 2 ? SG_SW(V, S, 2) : SG_SW(V, S, 4))
         if (variant == 1) {
             if (stats) SG_SWW(1, true); else SG_SWW(1, false);
@@ -908,7 +933,9 @@ cudaError_t sg_launch_sir_count_step(const SgTickArgs &a, int variant, bool stat
         }
 #undef SG_SWW
 #undef SG_SW
-        return cudaGetLastError();
+        const cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess || a.hybrid_rise <= 0) return err;
+        // hybrid: the loop form too (it returns at once in sweep ticks)
     }
     if (stats) { // statistics runs of the loop form use one flavour
         if (variant == 1) {

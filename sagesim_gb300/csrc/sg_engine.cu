@@ -566,6 +566,7 @@ static SgTickArgs base_args(sg_engine *e, SgStep *s, int32_t r, bool inplace)
     a.thread_row = e->tune.thread_row;
     a.flavour = e->tune.count_flavour;
     a.sweep_wpt = sg_sweep_wpt(s->ntiles, e->sm_count, a.flavour);
+    sg_hybrid_thresholds(s->ntiles, a.flavour, &a.hybrid_rise, &a.hybrid_fall);
     if ((a.flavour & SG_FLAVOUR_SWEEP) && !(a.flavour & SG_FLAVOUR_FORCE) &&
         s->ntiles < e->sm_count * SG_SWEEP_MIN_TILES_PER_SM)
         a.flavour = (a.flavour & ~SG_FLAVOUR_SWEEP) | SG_FLAVOUR_LAZY;

@@ -49,7 +49,9 @@ struct SgMega {
 #define SG_FLAVOUR_FORCE 32 // class sweep on any graph size (see below)
 #define SG_FLAVOUR_WPT_SHIFT 6 // bits 6-7: class-sweep warps per tile, 0 = automatic
                               // (sg_sweep_wpt), 1/2/3 = 1/2/4 warps
-#define SG_FLAVOUR_MAX 255
+#define SG_FLAVOUR_HYBRID 256 // class sweep in quiet ticks, the loop form (bits 0-2) in
+                              // busy ticks (see SgTickArgs::hybrid_rise/fall)
+#define SG_FLAVOUR_MAX 511
 // The class sweep runs one warp per tile; below this many tiles per SM it
 // leaves SMs idle and the loop form (lazy loads) is used instead, unless
 // SG_FLAVOUR_FORCE is set.
@@ -58,6 +60,17 @@ struct SgMega {
 // Warps per tile of the class sweep: one warp per tile while there are enough
 // tiles to give every SM its 4 resident blocks of 8 warps, else 2 or 4 warps
 // share a tile so that smaller graphs still fill the SMs.
+// Change-count thresholds of the hybrid count step for a launch over ntiles
+// tiles (the crossovers measured on a 10^7-agent power-law epidemic: about one
+// change per 400 agents while it grows, one per 36 while it declines).
+inline void sg_hybrid_thresholds(int64_t ntiles, int32_t flavour, int32_t *rise, int32_t *fall)
+{
+    const int64_t n = ntiles * SG_TILE;
+    const bool on = (flavour & SG_FLAVOUR_HYBRID) && (flavour & SG_FLAVOUR_SWEEP);
+    *rise = on ? (int32_t)(n / 400 > 0 ? n / 400 : 1) : 0;
+    *fall = on ? (int32_t)(n / 36 > 0 ? n / 36 : 1) : 0;
+}
+
 inline int32_t sg_sweep_wpt(int64_t ntiles, int sm_count, int32_t flavour)
 {
     const int32_t forced = (flavour >> SG_FLAVOUR_WPT_SHIFT) & 3;
@@ -119,6 +132,10 @@ struct SgTickArgs {
     int32_t *tick_cand;     // NULL, or [ticks] candidates the sweep processed at tick r
                             // (zero before the run)
     int32_t sweep_wpt;      // class sweep: warps per tile (1, 2 or 4; see sg_sweep_wpt)
+    int32_t hybrid_rise;    // hybrid count step (0 = off): tick r > 1 runs the loop form
+    int32_t hybrid_fall;    // when tick r - 1 recorded more than hybrid_rise changes and
+                            // no fewer than tick r - 2 (epidemic growing), or more than
+                            // hybrid_fall changes; the class sweep otherwise
     // frontier strategy
     int32_t *list[2];       // active agents of tick r in list[r & 1]
     int32_t *list_len;      // [ticks + 1] list lengths, slot r

@@ -82,7 +82,7 @@ def test_sir_matches_oracle_every_tick(variant, strategy, kind):
             st = ref
 
 
-COUNT_FLAVOURS = list(range(8)) + [8, 12, 16, 24, 48, 56, 63, 48 | 64, 48 | 128, 56 | 192]
+COUNT_FLAVOURS = list(range(8)) + [8, 12, 16, 24, 48, 56, 63, 48 | 64, 48 | 128, 56 | 192, 48 | 256 | 4, 48 | 256 | 1, 16 | 256]
 
 
 @pytest.mark.parametrize("flavour", COUNT_FLAVOURS)
@@ -108,7 +108,7 @@ def test_count_step_flavours_identical(flavour, variant):
     assert np.array_equal(got, ref)
 
 
-@pytest.mark.parametrize("flavour", [0, 16, 48, 48 | 64, 48 | 128])
+@pytest.mark.parametrize("flavour", [0, 16, 48, 48 | 64, 48 | 128, 48 | 256 | 4, 48 | 256 | 3])
 @pytest.mark.parametrize("variant", ["A", "B"])
 def test_count_dense_graph_with_statistics(flavour, variant):
     """A dense graph with many infected neighbours per agent and a small beta
@@ -131,7 +131,7 @@ def test_count_dense_graph_with_statistics(flavour, variant):
     assert np.array_equal(stats, rstats)
 
 
-@pytest.mark.parametrize("wpt_bits", [64, 128, 192])
+@pytest.mark.parametrize("wpt_bits", [64, 128, 192, 256 | 4, 256 | 64 | 2])
 @pytest.mark.parametrize("variant", ["A", "B"])
 def test_class_sweep_statistics_on_power_law_graph(variant, wpt_bits):
     """Class sweep with statistics on a graph with hubs, through busy and quiet
