@@ -139,7 +139,9 @@ typedef struct sg_tune {
                                /* bits 6-7: sweep warps per tile, 0 = automatic, */
                                /*      1/2/3 = 1/2/4 warps                       */
                                /* 256 = with 16: hybrid, the loop form of bits   */
-                               /*      0-2 in busy ticks (decided on the GPU)    */
+                               /*      0-2 in busy ticks (decided on the GPU;    */
+                               /*      graphs of 24+ tiles per SM, or with 32)   */
+                               /* default 272 (class sweep + hybrid)             */
     double us_per_tick;        /* measured by sg_batch_tune (output)             */
 } sg_tune;
 

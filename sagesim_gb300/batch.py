@@ -75,7 +75,7 @@ class Batch:
     def commit(self):
         self._ck(self._lib.sg_batch_commit(self._h))
 
-    def set_tune(self, strategy="count", blocks_per_sm=16, thread_row=32, mega_row=2048, count_flavour=16):
+    def set_tune(self, strategy="count", blocks_per_sm=16, thread_row=32, mega_row=2048, count_flavour=272):
         t = N.Tune(STRATEGIES[strategy], blocks_per_sm, thread_row, mega_row, count_flavour, 0.0)
         self._ck(self._lib.sg_batch_set_tune(self._h, ctypes.byref(t)))
 

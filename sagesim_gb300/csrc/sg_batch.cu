@@ -27,8 +27,16 @@ constexpr int32_t kLongRowFloor = 512; // rows kept as mega candidates (smallest
 // count-step flavours the autotuner times: loop form (4 or 8 agents per thread,
 // eager or lazy loads) and class sweep with the load-balanced scatter, and two
 // of them with the lane-per-row scatter
-constexpr int32_t kCountFlavourCands[] = {0, 1, 4, 5, SG_FLAVOUR_SWEEP, SG_FLAVOUR_SWEEP | SG_FLAVOUR_FORCE,
-                                          SG_FLAVOUR_ROWSCATTER | 4, SG_FLAVOUR_ROWSCATTER | SG_FLAVOUR_SWEEP};
+constexpr int32_t kCountFlavourCands[] = {0,
+                                          1,
+                                          4,
+                                          5,
+                                          SG_FLAVOUR_SWEEP,
+                                          SG_FLAVOUR_SWEEP | SG_FLAVOUR_FORCE,
+                                          SG_FLAVOUR_SWEEP | SG_FLAVOUR_HYBRID,
+                                          SG_FLAVOUR_SWEEP | SG_FLAVOUR_FORCE | SG_FLAVOUR_HYBRID,
+                                          SG_FLAVOUR_ROWSCATTER | 4,
+                                          SG_FLAVOUR_ROWSCATTER | SG_FLAVOUR_SWEEP};
 }
 
 int64_t SgRanges::take(int64_t len)
@@ -308,7 +316,7 @@ int SgPool::enqueue(int32_t nticks, bool capturing)
     a.thread_row = tune.thread_row;
     a.flavour = tune.count_flavour;
     a.sweep_wpt = sg_sweep_wpt((int64_t)htiles.size(), sm_count, a.flavour);
-    sg_hybrid_thresholds((int64_t)htiles.size(), a.flavour, &a.hybrid_rise, &a.hybrid_fall);
+    sg_hybrid_thresholds((int64_t)htiles.size(), sm_count, a.flavour, &a.hybrid_rise, &a.hybrid_fall);
     if ((a.flavour & SG_FLAVOUR_SWEEP) && !(a.flavour & SG_FLAVOUR_FORCE) &&
         (int64_t)htiles.size() < (int64_t)sm_count * SG_SWEEP_MIN_TILES_PER_SM)
         a.flavour = (a.flavour & ~SG_FLAVOUR_SWEEP) | SG_FLAVOUR_LAZY;

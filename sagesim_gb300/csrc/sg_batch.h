@@ -79,7 +79,7 @@ struct SgPool {
     bool tables_dirty = true;
     uint64_t version = 1;
 
-    sg_tune tune{SG_SIR_COUNT, 16, 32, 2048, SG_FLAVOUR_SWEEP, 0.0};
+    sg_tune tune{SG_SIR_COUNT, 16, 32, 2048, SG_FLAVOUR_SWEEP | SG_FLAVOUR_HYBRID, 0.0};
     cudaGraphExec_t graph = nullptr;
     int32_t graph_nticks = -1;
     uint64_t graph_version = 0;

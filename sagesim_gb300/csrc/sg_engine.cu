@@ -84,7 +84,7 @@ struct sg_engine {
 
     SgProfiler prof;
     int hub_deg = 32;
-    sg_tune tune{SG_SIR_COUNT, 16, 32, 2048, SG_FLAVOUR_SWEEP, 0.0};
+    sg_tune tune{SG_SIR_COUNT, 16, 32, 2048, SG_FLAVOUR_SWEEP | SG_FLAVOUR_HYBRID, 0.0};
     int32_t last_nticks = 0;
 
     // CUDA graph of the tick loop (sg_run_async with use_graph)
@@ -566,7 +566,7 @@ static SgTickArgs base_args(sg_engine *e, SgStep *s, int32_t r, bool inplace)
     a.thread_row = e->tune.thread_row;
     a.flavour = e->tune.count_flavour;
     a.sweep_wpt = sg_sweep_wpt(s->ntiles, e->sm_count, a.flavour);
-    sg_hybrid_thresholds(s->ntiles, a.flavour, &a.hybrid_rise, &a.hybrid_fall);
+    sg_hybrid_thresholds(s->ntiles, e->sm_count, a.flavour, &a.hybrid_rise, &a.hybrid_fall);
     if ((a.flavour & SG_FLAVOUR_SWEEP) && !(a.flavour & SG_FLAVOUR_FORCE) &&
         s->ntiles < e->sm_count * SG_SWEEP_MIN_TILES_PER_SM)
         a.flavour = (a.flavour & ~SG_FLAVOUR_SWEEP) | SG_FLAVOUR_LAZY;

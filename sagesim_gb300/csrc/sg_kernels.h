@@ -46,11 +46,12 @@ struct SgMega {
 #define SG_FLAVOUR_ROWSCATTER 8 // scatter walks one transpose row per lane instead of
                                 // the warp's rows laid end to end
 #define SG_FLAVOUR_SWEEP 16 // class sweep (in-place runs that keep class bytes)
-#define SG_FLAVOUR_FORCE 32 // class sweep on any graph size (see below)
+#define SG_FLAVOUR_FORCE 32 // class sweep (and hybrid) on any graph size (see below)
 #define SG_FLAVOUR_WPT_SHIFT 6 // bits 6-7: class-sweep warps per tile, 0 = automatic
                               // (sg_sweep_wpt), 1/2/3 = 1/2/4 warps
 #define SG_FLAVOUR_HYBRID 256 // class sweep in quiet ticks, the loop form (bits 0-2) in
-                              // busy ticks (see SgTickArgs::hybrid_rise/fall)
+                              // busy ticks (see SgTickArgs::hybrid_rise/fall and
+                              // sg_hybrid_thresholds)
 #define SG_FLAVOUR_MAX 511
 // The class sweep runs one warp per tile; below this many tiles per SM it
 // leaves SMs idle and the loop form (lazy loads) is used instead, unless
@@ -62,11 +63,16 @@ struct SgMega {
 // share a tile so that smaller graphs still fill the SMs.
 // Change-count thresholds of the hybrid count step for a launch over ntiles
 // tiles (the crossovers measured on a 10^7-agent power-law epidemic: about one
-// change per 400 agents while it grows, one per 36 while it declines).
-inline void sg_hybrid_thresholds(int64_t ntiles, int32_t flavour, int32_t *rise, int32_t *fall)
+// change per 400 agents while it grows, one per 36 while it declines). The
+// unchosen kernel's launch costs about 2.5 us per tick, which smaller graphs
+// do not earn back (measured at 10^6 and 2.5 10^6 agents), so the hybrid runs
+// from SG_HYBRID_MIN_TILES_PER_SM tiles per SM.
+#define SG_HYBRID_MIN_TILES_PER_SM 24
+inline void sg_hybrid_thresholds(int64_t ntiles, int sm_count, int32_t flavour, int32_t *rise, int32_t *fall)
 {
     const int64_t n = ntiles * SG_TILE;
-    const bool on = (flavour & SG_FLAVOUR_HYBRID) && (flavour & SG_FLAVOUR_SWEEP);
+    const bool on = (flavour & SG_FLAVOUR_HYBRID) && (flavour & SG_FLAVOUR_SWEEP) &&
+                    ((flavour & SG_FLAVOUR_FORCE) || ntiles >= (int64_t)sm_count * SG_HYBRID_MIN_TILES_PER_SM);
     *rise = on ? (int32_t)(n / 400 > 0 ? n / 400 : 1) : 0;
     *fall = on ? (int32_t)(n / 36 > 0 ? n / 36 : 1) : 0;
 }

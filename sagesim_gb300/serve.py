@@ -80,7 +80,7 @@ class Server:
                                             ctypes.byref(b)))
         return {"queued": q.value, "resident": r.value, "done": d.value, "resident_bytes": b.value}
 
-    def set_tune(self, strategy="count", blocks_per_sm=16, thread_row=32, mega_row=2048, count_flavour=16):
+    def set_tune(self, strategy="count", blocks_per_sm=16, thread_row=32, mega_row=2048, count_flavour=272):
         t = N.Tune(STRATEGIES[strategy], blocks_per_sm, thread_row, mega_row, count_flavour, 0.0)
         self._ck(self._lib.sg_server_set_tune(self._h, ctypes.byref(t)))
 
