@@ -37,6 +37,13 @@ TICKS = 200
 BETA, GAMMA = 0.03, 0.07
 INFECTED_FRAC = 0.001
 SEED = 1
+# DRAM traffic per launch of the dominant kernel (dram__bytes_read.sum +
+# dram__bytes_write.sum, averaged over all 200 ticks of one simulate), from
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum \
+#       --clock-control none --csv --log-file dram.csv python bench.py --profile-case
+# keyed by (strategy, agents, kernel); the count step is the sum of both hybrid kernels
+# per tick. Re-measure when a kernel changes.
+MEASURED_TRAFFIC = {("count", 10_000_000, "sir_count_step"): 56.975e6}
 PARTS = 64
 CODES = (1, 2, 3)
 
@@ -497,7 +504,8 @@ def main():
             eng.add_sir(prop, BETA, GAMMA, variant="B", strategy=strategy, codes=CODES)
             eng.snapshot()
             # trajectory statistics (untimed): E_S per tick for edge-visits/s and bytes
-            tick_stats, _ = eng.run(0, TICKS, stats=True)
+            tick_stats, totals = eng.run(0, TICKS, stats=True)
+            run_launches = int(totals.kernel_launches)
             active = eng.last_run_active(TICKS).astype(np.float64)
             final = eng.get_property(prop)
             eng.restore()
@@ -553,21 +561,29 @@ def main():
             eng.profile(False)
             eng.close()
         dom_name, (dom_launches, dom_ms) = max(rep.items(), key=lambda kv: kv[1][1])
-        alg = algorithmic_bytes(dom_name, n, st0, tick_stats, active)
         E_S = tick_stats[:, 3].astype(np.float64)
-        alg_per_launch = float(alg.mean())
         per_launch_ms = dom_ms / max(dom_launches, 1)
-        achieved = alg_per_launch / (per_launch_ms / 1e3) / 1e9
-        kernels_per_tick = 1 if strategy == "pull" else 2
-        setup_launches = {"pull": 0, "count": 1, "frontier": 2}[strategy]
+        # the contract's algorithmic bytes: one SIR tick of the reference's scan,
+        # 12 N + 4 + 4 E_S (state read and write and row offset per agent, one CSR
+        # index per neighbour of each susceptible agent); one launch of the
+        # dominant step kernel advances one tick
+        ref_bytes = float((12.0 * n + 4.0 + 4.0 * E_S).mean())
+        achieved = ref_bytes / (per_launch_ms / 1e3) / 1e9
+        # the kernel's own compulsory bytes (it does not scan rows; see algorithmic_bytes)
+        own = float(algorithmic_bytes(dom_name, n, st0, tick_stats, active).mean())
+        own_achieved = own / (per_launch_ms / 1e3) / 1e9
+        traffic = MEASURED_TRAFFIC.get((strategy, n, dom_name))
         return {
             "value": world * n * TICKS / (ms_step / 1e3), "ms_per_step": ms_step,
             "e2e": world * n * TICKS / e2e_s, "edge_visits_per_s": world * float(E_S.sum()) / (ms_step / 1e3),
-            "launches": steps * (TICKS * kernels_per_tick + setup_launches),
+            "launches": steps * run_launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "kernel": dom_name,
+                         "frac": achieved / peak, "traffic": traffic, "kernel": dom_name,
                          "peak_source": peak_kind, "per_launch_us": per_launch_ms * 1e3,
-                         "alg_bytes_per_launch": alg_per_launch},
+                         "alg_bytes_per_launch": ref_bytes,
+                         "alg_bytes": "12N + 4 + 4 E_S per tick (one tick of the reference scan)",
+                         "kernel_bytes_per_launch": own, "kernel_achieved": own_achieved,
+                         "kernel_frac": own_achieved / peak},
             "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in rep.items()},
             "clocks": clocks, "final": final,
         }

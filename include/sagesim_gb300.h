@@ -120,6 +120,7 @@ typedef struct sg_stats {
     int64_t edge_visits;    /* sum over ticks of E_S (degree sum of the agents
                                susceptible at tick start); SIR only             */
     double device_ms;       /* device time of the run (CUDA events)             */
+    int64_t kernel_launches; /* kernels the run launched                        */
 } sg_stats;
 
 /* Launch configuration the autotuner chooses between (all give identical results). */

@@ -69,7 +69,8 @@ class BuiltinParams(ctypes.Structure):
 
 class Stats(ctypes.Structure):
     _fields_ = [("ticks", ctypes.c_int64), ("agent_ticks", ctypes.c_int64),
-                ("edge_visits", ctypes.c_int64), ("device_ms", ctypes.c_double)]
+                ("edge_visits", ctypes.c_int64), ("device_ms", ctypes.c_double),
+                ("kernel_launches", ctypes.c_int64)]
 
 
 class ScenarioDesc(ctypes.Structure):

@@ -915,9 +915,10 @@ static void count_step_flavour(const SgTickArgs &a, int flavour, int grid, cudaS
 }
 
 cudaError_t sg_launch_sir_count_step(const SgTickArgs &args, int variant, bool stats, bool inplace,
-                                     int grid, cudaStream_t st)
+                                     int grid, cudaStream_t st, int *nlaunched)
 {
     SgTickArgs a = args;
+    if (nlaunched) *nlaunched = 1;
     const bool sweep = (a.flavour & SG_FLAVOUR_SWEEP) && inplace && a.cls && a.chunks;
     if (!sweep) a.hybrid_rise = 0; // the loop form takes every tick
     if (sweep) {
@@ -935,6 +936,7 @@ cudaError_t sg_launch_sir_count_step(const SgTickArgs &args, int variant, bool s
 #undef SG_SW
         const cudaError_t err = cudaGetLastError();
         if (err != cudaSuccess || a.hybrid_rise <= 0) return err;
+        if (nlaunched) *nlaunched = 2;
         // hybrid: the loop form too (it returns at once in sweep ticks)
     }
     if (stats) { // statistics runs of the loop form use one flavour

@@ -86,6 +86,7 @@ struct sg_engine {
     int hub_deg = 32;
     sg_tune tune{SG_SIR_COUNT, 16, 32, 2048, SG_FLAVOUR_SWEEP | SG_FLAVOUR_HYBRID, 0.0};
     int32_t last_nticks = 0;
+    int64_t last_launches = 0; // kernels launched by the last enqueued run
 
     // CUDA graph of the tick loop (sg_run_async with use_graph)
     cudaGraphExec_t graph_exec = nullptr;
@@ -617,12 +618,14 @@ static int grid_for(sg_engine *e, int32_t ntiles)
         cudaError_t _ce = (launch_expr);                                                       \
         if (_ce != cudaSuccess) return e->cuda_fail(_ce, kindname);                            \
         if (_p) e->prof.end(_tok, e->stream);                                                  \
+        ++e->last_launches;                                                                    \
     } while (0)
 
 // Enqueues nticks ticks (relative ticks 0..nticks-1) for the prepared steps.
 static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool stats_on,
                          bool capturing)
 {
+    e->last_launches = 0;
     const int grid_sc = e->sm_count * 16;
     if (pl.frontier) {
         SgStep *s = pl.count_step;
@@ -673,7 +676,10 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
             if (s->kind == SG_BUILTIN_SIR_A || s->kind == SG_BUILTIN_SIR_B) {
                 const int variant = s->kind == SG_BUILTIN_SIR_A ? 1 : 2;
                 if (s->bp.strategy == SG_SIR_COUNT) {
-                    SG_PROF_LAUNCH("sir_count_step", sg_launch_sir_count_step(a, variant, stats_on, inplace, grid, e->stream));
+                    int nk = 1;
+                    SG_PROF_LAUNCH("sir_count_step",
+                                   sg_launch_sir_count_step(a, variant, stats_on, inplace, grid, e->stream, &nk));
+                    e->last_launches += nk - 1;
                     SG_PROF_LAUNCH("sir_count_scatter", sg_launch_sir_count_scatter(a, grid_sc, e->stream));
                 } else {
                     SG_PROF_LAUNCH("sir_pull",
@@ -854,6 +860,7 @@ int sg_run(sg_engine *e, int64_t tick0, int32_t nticks, int64_t *tick_stats, sg_
         for (int32_t r = 0; r < nticks; ++r) ev += (int64_t)st[(size_t)r * 4 + 3];
         out->edge_visits = ev;
         out->device_ms = ms;
+        out->kernel_launches = e->last_launches;
     }
     return SG_OK;
 }

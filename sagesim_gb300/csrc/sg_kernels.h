@@ -162,8 +162,9 @@ cudaError_t sg_launch_sir_count_init(const SgTickArgs &a, int grid, cudaStream_t
 // inplace: the state buffer is read and written in place (buf0); only changed
 // agents are stored. Valid when the count step is the engine's only step, since
 // it reads nothing but the agent's own state and count.
+// nlaunched (optional): kernels launched (2 for the hybrid step, else 1).
 cudaError_t sg_launch_sir_count_step(const SgTickArgs &a, int variant, bool stats, bool inplace,
-                                     int grid, cudaStream_t st);
+                                     int grid, cudaStream_t st, int *nlaunched = nullptr);
 cudaError_t sg_launch_sir_count_scatter(const SgTickArgs &a, int grid, cudaStream_t st);
 // Frontier strategy (state in buf0, updated in place). list_len[0..ticks] and
 // nch[0..ticks-1] must be zero before the build.
