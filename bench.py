@@ -226,6 +226,76 @@ def ensemble_section(stream, steps, device=0, ticks=365):
             "tune": tune, "bit_exact_scenarios": len(gs) - mismatches, "device_bytes": info["device_bytes"]}
 
 
+def opinion_section(stream, steps, device=0, peak=None, n=2_000_000, ticks=500):
+    """Config 3: opinion dynamics on WS n=2e6 k=10 p=0.1 (seed 2, ordered rows),
+    opinions U[0,1), float32[8] weights N(0,1), noise sigma 0.01, 500 ticks.
+
+    Returns agent-ticks/s (device, graph replay), the opinion kernel's roofline on
+    its algorithmic bytes per tick (4N opinion read + 4N write + 32N weights + 4N
+    row offsets + 4E neighbour indices, neighbour opinions counted as reuse), the
+    largest relative difference from the oracle after 20 ticks, and the oracle's
+    rate on the host cores."""
+    import torch
+
+    from oracle import oracle
+    from sagesim_gb300 import Engine, graphs
+
+    off, idx = graphs.watts_strogatz(n, 10, 0.1, 2)
+    rng = np.random.default_rng(2)
+    x0 = rng.random(n, dtype=np.float32)
+    w = rng.standard_normal((n, 8), dtype=np.float32)
+    nnz = int(off[-1])
+    with torch.cuda.stream(stream):
+        eng = Engine(device=device, stream=stream.cuda_stream)
+        eng.set_graph(off, idx, ordered=True)
+        eng.set_seed(2)
+        px = eng.add_property("opinion", np.float32, init=x0)
+        pw = eng.add_property("weights", np.float32, width=8, init=w)
+        eng.add_opinion(px, pw, 0.01)
+        eng.snapshot()
+        eng.run(0, 20, stats=False)
+        got20 = eng.get_property(px)
+        for _ in range(2):
+            eng.restore()
+            eng.run_async(0, ticks, use_graph=True)
+        stream.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(steps):
+            eng.restore()
+            eng.run_async(0, ticks, use_graph=True)
+        ev1.record(stream)
+        stream.synchronize()
+        ms = ev0.elapsed_time(ev1) / steps
+        eng.restore()
+        eng.profile(True)
+        eng.run(0, ticks, stats=False)
+        rep = eng.profile_report()
+        eng.profile(False)
+        eng.close()
+    want20, _ = oracle.opinion_run(off, idx, w, x0, 2, 0, 20, 0.01)
+    rel = np.abs(got20 - want20) / np.maximum(np.abs(want20), 1e-30)
+    rel = np.where(np.abs(got20 - want20) <= 1e-12, 0.0, rel)
+    t0 = time.perf_counter()
+    oracle.opinion_run(off, idx, w, x0, 2, 0, 20, 0.01)
+    cpu_dt = time.perf_counter() - t0
+    launches, k_ms = rep.get("opinion", (ticks, ms))
+    per_launch_s = k_ms / max(launches, 1) / 1e3
+    alg = 4.0 * n + 4.0 * n + 32.0 * n + 4.0 * n + 4.0 * nnz
+    achieved = alg / per_launch_s / 1e9
+    out = {"workload": "opinion, WS n=2e6 k=10 p=0.1 seed 2 (ordered), float32[8] weights, sigma 0.01, "
+                       "%d ticks" % ticks,
+           "agent_ticks_per_s": n * ticks / (ms / 1e3), "ms_per_step": ms, "nnz": nnz,
+           "max_rel_diff_vs_oracle_20_ticks": float(rel.max()), "within_1e-6": bool(rel.max() <= 1e-6),
+           "roofline": {"bound": "hbm", "achieved": achieved, "unit": "GB/s", "per_launch_us": per_launch_s * 1e6,
+                        "alg_bytes_per_launch": alg},
+           "cpu_port_agent_ticks_per_s": n * 20 / cpu_dt, "cpu_cores": oracle.max_threads()}
+    if peak:
+        out["roofline"]["peak"] = peak
+        out["roofline"]["frac"] = achieved / peak
+    return out
+
+
 def serving_section(stream, device=0, n_requests=100, n_graphs=24):
     """Config 5 scaled to n_requests: Poisson arrivals at 200 req/s (seed 4),
     n log-uniform in [1e4, 5e6], BA or ER with mean degree 4..16, horizons
@@ -599,7 +669,8 @@ def main():
     extra = {}
     if rank == 0 and not args.no_extras:
         for name, fn in (("ensemble", lambda: ensemble_section(stream, max(1, min(args.steps, 3)), local)),
-                         ("serving", lambda: serving_section(stream, local))):
+                         ("serving", lambda: serving_section(stream, local)),
+                         ("opinion", lambda: opinion_section(stream, max(1, min(args.steps, 3)), local, peak))):
             try:
                 extra[name] = fn()
             except Exception as exc:  # a failing extra section must not lose the headline line

@@ -80,6 +80,8 @@ struct sg_engine {
     bool last_sweep = false; // the last run's count step was the class sweep
     SgDev flist[2], flen, fnch, fmark, fstats_init, fstats_delta; // frontier strategy
     SgDev transpose_tmp, scan_tmp;
+    SgDev bm_radius, bm_cos; // opinion: Box-Muller tables, built once per engine
+    bool bm_ready = false;
     SgDev prop_table; // sg_prop_dev per property, for compiled steps
 
     SgProfiler prof;
@@ -686,7 +688,9 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
                                    sg_launch_sir_pull(a, variant, stats_on, grid + a.mega_blocks, e->stream));
                 }
             } else if (s->kind == SG_BUILTIN_OPINION) {
-                SG_PROF_LAUNCH("opinion", sg_launch_opinion(a, grid, e->stream));
+                a.bm_radius = e->bm_ready ? e->bm_radius.as<double>() : nullptr;
+                a.bm_cos = e->bm_ready ? e->bm_cos.as<double>() : nullptr;
+                SG_PROF_LAUNCH("opinion", sg_launch_opinion(a, grid, e->stream, s->host_seg.width));
             } else {
                 sg_step_args L{};
                 L.tiles = (const int *)s->tiles.p;
@@ -762,6 +766,12 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
     for (SgStep *s : pl.order) {
         rc = prepare_step(e, s, tick0, stats);
         if (rc) return rc;
+        if (s->kind == SG_BUILTIN_OPINION && !e->bm_ready) { // before any capture
+            SG_CK(e->bm_radius.reserve((size_t)SG_BOX_MULLER_SIZE * sizeof(double)));
+            SG_CK(e->bm_cos.reserve((size_t)SG_BOX_MULLER_SIZE * sizeof(double)));
+            SG_CK(sg_launch_opinion_tables(e->bm_radius.as<double>(), e->bm_cos.as<double>(), e->stream));
+            e->bm_ready = true;
+        }
     }
     if (pl.count_step) {
         SG_CK(e->tile_nch.reserve((size_t)std::max(pl.count_step->ntiles, 1) * 4));

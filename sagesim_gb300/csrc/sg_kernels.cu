@@ -370,7 +370,74 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) frontier_scatter_kernel(SgTick
 // x' = clamp((double)(sum_j w_j x_nbr_j / sum_j |w_j|) + sigma * N(0,1), 0, 1)
 // over the first min(deg, width) ordered neighbours; float32 sums in row order
 // with every multiply and add rounded (no FMA), Box-Muller in double
-// (sagesim/math_utils.py:231-255: u1 salt 1, u2 salt 1 + 73856093, +1e-10 guard).
+// (sagesim/math_utils.py:231-255: u1 salt 1, u2 salt 1 + 73856093, +1e-10
+// guard). u1 and u2 are k / 2^23 for 23-bit Philox integers k, so
+// sqrt(-2 log(u1 + 1e-10)) and cos(2 pi u2) take 2^23 values each: they are
+// tabulated once (opinion_tables_kernel, the same double expressions) and an
+// agent's normal is two table reads and one multiply, bit for bit the same as
+// evaluating it -- the double-precision transcendentals otherwise cost ten
+// times the tick's memory traffic. (A float32 Box-Muller was tried and
+// rejected: opinions near the clamp at 0 differ by up to 1.5e-4 relative.)
+constexpr int32_t kBoxMullerSize = 1 << 23;
+
+__device__ __forceinline__ double bm_radius(uint32_t k)
+{
+    const double u1 = (double)k / 8388608.0;
+    return sqrt(__dmul_rn(-2.0, log(__dadd_rn(u1, 1e-10))));
+}
+
+__device__ __forceinline__ double bm_cos(uint32_t k)
+{
+    const double u2 = (double)k / 8388608.0;
+    return cos(__dmul_rn(6.283185307179586, u2));
+}
+
+__global__ void opinion_tables_kernel(double *__restrict__ radius, double *__restrict__ cosine)
+{
+    for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < kBoxMullerSize; k += gridDim.x * blockDim.x) {
+        radius[k] = bm_radius((uint32_t)k);
+        cosine[k] = bm_cos((uint32_t)k);
+    }
+}
+// All of a row's loads are issued before the sums: for width 8 the weight row
+// is two 16-byte loads, then the (up to 8) neighbour indices, then their opinions.
+template <int W> // 8, or 0 for any width
+__device__ __forceinline__ float opinion_mean(const SgTickArgs &a, const SgSeg &sg, const float *__restrict__ xin,
+                                              int32_t i, int32_t width)
+{
+    const int32_t b = __ldg(a.off + i);
+    int32_t m = __ldg(a.off + i + 1) - b;
+    if (m > width) m = width;
+    float acc = 0.0f, norm = 0.0f;
+    if (W == 8) {
+        const float4 *w4 = reinterpret_cast<const float4 *>(sg.weights + (int64_t)i * 8);
+        const float4 w0 = __ldg(w4), w1 = __ldg(w4 + 1);
+        const float wv[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+        int32_t nb[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) nb[j] = j < m ? __ldg(a.idx + b + j) : i;
+        float xv[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) xv[j] = __ldg(xin + nb[j]);
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (j < m) {
+                acc = __fadd_rn(acc, __fmul_rn(wv[j], xv[j]));
+                norm = __fadd_rn(norm, fabsf(wv[j]));
+            }
+    } else {
+        const float *__restrict__ w = sg.weights + (int64_t)i * width;
+        for (int32_t j = 0; j < m; ++j) {
+            const float wj = __ldg(w + j);
+            const float xj = __ldg(xin + __ldg(a.idx + b + j));
+            acc = __fadd_rn(acc, __fmul_rn(wj, xj));
+            norm = __fadd_rn(norm, fabsf(wj));
+        }
+    }
+    return norm > 0.0f ? __fdiv_rn(acc, norm) : xin[i];
+}
+
+template <int W>
 __global__ void __launch_bounds__(SG_SIR_THREADS) opinion_kernel(SgTickArgs a)
 {
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
@@ -384,25 +451,13 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) opinion_kernel(SgTickArgs a)
         const uint32_t c0b = sg_c0base(tick);
         const int32_t width = sg.width;
         for (int32_t i = tile.begin + threadIdx.x; i < tile.end; i += SG_SIR_THREADS) {
-            const int32_t b = __ldg(a.off + i);
-            int32_t m = __ldg(a.off + i + 1) - b;
-            if (m > width) m = width;
-            const float *__restrict__ w = sg.weights + (int64_t)i * width;
-            float acc = 0.0f, norm = 0.0f;
-            for (int32_t j = 0; j < m; ++j) {
-                const float wj = __ldg(w + j);
-                const float xj = __ldg(xin + __ldg(a.idx + b + j));
-                acc = __fadd_rn(acc, __fmul_rn(wj, xj));
-                norm = __fadd_rn(norm, fabsf(wj));
-            }
-            float x = xin[i];
-            if (norm > 0.0f) x = __fdiv_rn(acc, norm);
+            const float x = opinion_mean<W>(a, sg, xin, i, width);
             const uint32_t lid = seg_lid(sg, i);
-            const double u1 = (double)sg_philox_k23(c0b + 1u, lid, sg.key) / 8388608.0;
-            const double u2 =
-                (double)sg_philox_k23(c0b + 1u + kNormalSalt2, lid, sg.key) / 8388608.0;
-            const double r = sqrt(__dmul_rn(-2.0, log(__dadd_rn(u1, 1e-10))));
-            const double z = __dmul_rn(r, cos(__dmul_rn(6.283185307179586, u2)));
+            const uint32_t k1 = sg_philox_k23(c0b + 1u, lid, sg.key);
+            const uint32_t k2 = sg_philox_k23(c0b + 1u + kNormalSalt2, lid, sg.key);
+            const double r = a.bm_radius ? __ldg(a.bm_radius + k1) : bm_radius(k1);
+            const double c = a.bm_cos ? __ldg(a.bm_cos + k2) : bm_cos(k2);
+            const double z = __dmul_rn(r, c);
             double y = __dadd_rn((double)x, __dmul_rn(sg.sigma, z));
             if (y < 0.0) y = 0.0;
             if (y > 1.0) y = 1.0;
@@ -467,9 +522,20 @@ cudaError_t sg_launch_sir_pull(const SgTickArgs &a, int variant, bool stats, int
     return cudaGetLastError();
 }
 
-cudaError_t sg_launch_opinion(const SgTickArgs &a, int grid, cudaStream_t st)
+cudaError_t sg_launch_opinion_tables(double *radius, double *cosine, cudaStream_t st)
 {
-    opinion_kernel<<<grid, SG_SIR_THREADS, 0, st>>>(a);
+    opinion_tables_kernel<<<152 * 8, 256, 0, st>>>(radius, cosine);
+    return cudaGetLastError();
+}
+
+// width: the weights per agent of every segment of the launch (8 takes the
+// vector-load path).
+cudaError_t sg_launch_opinion(const SgTickArgs &a, int grid, cudaStream_t st, int width)
+{
+    if (width == 8)
+        opinion_kernel<8><<<grid, SG_SIR_THREADS, 0, st>>>(a);
+    else
+        opinion_kernel<0><<<grid, SG_SIR_THREADS, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -138,6 +138,8 @@ struct SgTickArgs {
     int32_t *tick_cand;     // NULL, or [ticks] candidates the sweep processed at tick r
                             // (zero before the run)
     int32_t sweep_wpt;      // class sweep: warps per tile (1, 2 or 4; see sg_sweep_wpt)
+    const double *bm_radius; // opinion: NULL, or the 2^23-entry Box-Muller tables of
+    const double *bm_cos;    // sg_launch_opinion_tables
     int32_t hybrid_rise;    // hybrid count step (0 = off): tick r > 1 runs the loop form
     int32_t hybrid_fall;    // when tick r - 1 recorded more than hybrid_rise changes and
                             // no fewer than tick r - 2 (epidemic growing), or more than
@@ -171,7 +173,11 @@ cudaError_t sg_launch_sir_count_scatter(const SgTickArgs &a, int grid, cudaStrea
 cudaError_t sg_launch_frontier_build(const SgTickArgs &a, bool stats, int grid, cudaStream_t st);
 cudaError_t sg_launch_frontier_step(const SgTickArgs &a, int variant, bool stats, int grid, cudaStream_t st);
 cudaError_t sg_launch_frontier_scatter(const SgTickArgs &a, int grid, cudaStream_t st);
-cudaError_t sg_launch_opinion(const SgTickArgs &a, int grid, cudaStream_t st);
+cudaError_t sg_launch_opinion(const SgTickArgs &a, int grid, cudaStream_t st, int width);
+// Fills the opinion step's Box-Muller tables, 2^23 doubles each (64 MiB each):
+// radius[k] = sqrt(-2 log(k / 2^23 + 1e-10)), cosine[k] = cos(2 pi k / 2^23).
+#define SG_BOX_MULLER_SIZE (1 << 23)
+cudaError_t sg_launch_opinion_tables(double *radius, double *cosine, cudaStream_t st);
 // Adds edge_base to off[0..n1) and agent_base to idx[0..nnz) in place (placing a
 // scenario's local CSR into a pool).
 cudaError_t sg_launch_offset_csr(int32_t *off, int64_t n1, int32_t edge_base, int32_t *idx, int64_t nnz,
