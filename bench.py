@@ -473,6 +473,26 @@ def profile_case(args):
             print("tick %3d  S %9d  I %9d  R %9d  E_S %10d  processed %9d" % ((t,) + tuple(stats[t]) + (active[t],)))
 
 
+def profile_opinion(args):
+    """Thirty ticks of the opinion workload (WS n=2e6), no timing: the command ncu wraps."""
+    from sagesim_gb300 import Engine, graphs
+
+    n = 2_000_000
+    off, idx = graphs.watts_strogatz(n, 10, 0.1, 2)
+    rng = np.random.default_rng(2)
+    x0 = rng.random(n, dtype=np.float32)
+    w = rng.standard_normal((n, 8), dtype=np.float32)
+    with Engine() as eng:
+        eng.set_graph(off, idx, ordered=True)
+        eng.set_seed(2)
+        px = eng.add_property("opinion", np.float32, init=x0)
+        pw = eng.add_property("weights", np.float32, width=8, init=w)
+        eng.add_opinion(px, pw, 0.01)
+        eng.run(0, 30, stats=False)
+        out = eng.get_property(px)
+    print("opinion profile case done: %d agents, 30 ticks, mean opinion %.6f" % (n, float(out.mean())))
+
+
 def sweep(args):
     """Device time of simulate(200) for every count-step launch configuration."""
     import torch
@@ -530,6 +550,8 @@ def main():
                     help="time every count-step flavour x blocks/SM on the workload and exit")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the ensemble and serving sections")
+    ap.add_argument("--profile-opinion", action="store_true",
+                    help="run 30 ticks of the opinion workload and exit (for ncu captures)")
     ap.add_argument("--profile-case", action="store_true",
                     help="run one simulate(200) of --strategy and exit (for ncu captures)")
     args = ap.parse_args()
@@ -538,6 +560,9 @@ def main():
         return
     if args.profile_case:
         profile_case(args)
+        return
+    if args.profile_opinion:
+        profile_opinion(args)
         return
     if args.sweep:
         sweep(args)

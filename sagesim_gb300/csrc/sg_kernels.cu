@@ -410,12 +410,14 @@ __device__ __forceinline__ float opinion_mean(const SgTickArgs &a, const SgSeg &
     if (m > width) m = width;
     float acc = 0.0f, norm = 0.0f;
     if (W == 8) {
+        // weights, row indices and the Box-Muller tables are read once per tick:
+        // evict-first loads keep L2 for the opinions, which neighbours re-read
         const float4 *w4 = reinterpret_cast<const float4 *>(sg.weights + (int64_t)i * 8);
-        const float4 w0 = __ldg(w4), w1 = __ldg(w4 + 1);
+        const float4 w0 = __ldcs(w4), w1 = __ldcs(w4 + 1);
         const float wv[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
         int32_t nb[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) nb[j] = j < m ? __ldg(a.idx + b + j) : i;
+        for (int j = 0; j < 8; ++j) nb[j] = j < m ? __ldcs(a.idx + b + j) : i;
         float xv[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) xv[j] = __ldg(xin + nb[j]);
@@ -455,8 +457,8 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) opinion_kernel(SgTickArgs a)
             const uint32_t lid = seg_lid(sg, i);
             const uint32_t k1 = sg_philox_k23(c0b + 1u, lid, sg.key);
             const uint32_t k2 = sg_philox_k23(c0b + 1u + kNormalSalt2, lid, sg.key);
-            const double r = a.bm_radius ? __ldg(a.bm_radius + k1) : bm_radius(k1);
-            const double c = a.bm_cos ? __ldg(a.bm_cos + k2) : bm_cos(k2);
+            const double r = a.bm_radius ? __ldcs(a.bm_radius + k1) : bm_radius(k1);
+            const double c = a.bm_cos ? __ldcs(a.bm_cos + k2) : bm_cos(k2);
             const double z = __dmul_rn(r, c);
             double y = __dadd_rn((double)x, __dmul_rn(sg.sigma, z));
             if (y < 0.0) y = 0.0;
