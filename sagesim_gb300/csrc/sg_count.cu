@@ -886,6 +886,31 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_scatter_kernel(SgTic
 
 } // namespace
 
+// Launches kernel k(a) with an L2 access-policy window over the counts when
+// a.cnt_window is set: the scatter's random +-1 updates and the steps' count
+// reads then find cnt in L2 instead of competing with the streamed arrays.
+static void launch_count_kernel(void (*k)(SgTickArgs), const SgTickArgs &a, int grid, cudaStream_t st)
+{
+    if (!a.cnt_window) {
+        k<<<grid, SG_SIR_THREADS, 0, st>>>(a);
+        return;
+    }
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(SG_SIR_THREADS);
+    cfg.stream = st;
+    cudaLaunchAttribute at{};
+    at.id = cudaLaunchAttributeAccessPolicyWindow;
+    at.val.accessPolicyWindow.base_ptr = a.cnt;
+    at.val.accessPolicyWindow.num_bytes = a.cnt_window;
+    at.val.accessPolicyWindow.hitRatio = 1.0f;
+    at.val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    at.val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    cfg.attrs = &at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, a);
+}
+
 cudaError_t sg_launch_sir_count_init(const SgTickArgs &a, int grid, cudaStream_t st)
 {
     sir_count_init_kernel<<<grid, SG_SIR_THREADS, 0, st>>>(a);
@@ -897,7 +922,7 @@ static void count_step_flavour(const SgTickArgs &a, int flavour, int grid, cudaS
 {
     const bool per8 = flavour & SG_FLAVOUR_PER8, lazy = flavour & SG_FLAVOUR_LAZY;
     const bool dense = V == 2 && (flavour & SG_FLAVOUR_DENSE);
-#define SG_CF(N, D, L) sir_count_step_kernel<V, false, P, N, D, L><<<grid, SG_SIR_THREADS, 0, st>>>(a)
+#define SG_CF(N, D, L) launch_count_kernel(sir_count_step_kernel<V, false, P, N, D, L>, a, grid, st)
     if (per8) {
         if (dense) {
             if (lazy) SG_CF(8, true, true); else SG_CF(8, true, false);
@@ -925,7 +950,7 @@ cudaError_t sg_launch_sir_count_step(const SgTickArgs &args, int variant, bool s
         const int wpt = a.sweep_wpt == 2 || a.sweep_wpt == 4 ? a.sweep_wpt : 1;
         const int tpb = kWarps / wpt;
         const int sgrid = std::max(1, std::min(grid, (a.ntiles + tpb - 1) / tpb)); // one group of tpb tiles per block
-#define SG_SW(V, S, W) sir_count_sweep_kernel<V, S, W><<<sgrid, SG_SIR_THREADS, 0, st>>>(a)
+#define SG_SW(V, S, W) launch_count_kernel(sir_count_sweep_kernel<V, S, W>, a, sgrid, st)
 #define SG_SWW(V, S) (wpt == 1 ? SG_SW(V, S, 1) : wpt == 2 ? SG_SW(V, S, 2) : SG_SW(V, S, 4))
         if (variant == 1) {
             if (stats) SG_SWW(1, true); else SG_SWW(1, false);
@@ -965,8 +990,8 @@ cudaError_t sg_launch_sir_count_scatter(const SgTickArgs &args, int grid, cudaSt
     if (!(a.flavour & SG_FLAVOUR_SWEEP)) a.amask = nullptr; // only the class sweep reads the bits
     const bool lb = !(a.flavour & SG_FLAVOUR_ROWSCATTER);
     if (a.chunks) {
-        if (lb) sir_count_scatter_chunks_kernel<true><<<grid, SG_SIR_THREADS, 0, st>>>(a);
-        else sir_count_scatter_chunks_kernel<false><<<grid, SG_SIR_THREADS, 0, st>>>(a);
+        if (lb) launch_count_kernel(sir_count_scatter_chunks_kernel<true>, a, grid, st);
+        else launch_count_kernel(sir_count_scatter_chunks_kernel<false>, a, grid, st);
     } else {
         if (lb) sir_count_scatter_kernel<true><<<grid, SG_SIR_THREADS, 0, st>>>(a);
         else sir_count_scatter_kernel<false><<<grid, SG_SIR_THREADS, 0, st>>>(a);

@@ -55,6 +55,7 @@ struct sg_engine {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int sm_count = 152;
+    size_t l2_window_max = 0; // largest access-policy window (bytes), 0 = unsupported
     std::string err;
 
     int64_t n = -1, nnz = 0;
@@ -82,6 +83,7 @@ struct sg_engine {
     SgDev transpose_tmp, scan_tmp;
     SgDev bm_radius, bm_cos; // opinion: Box-Muller tables, built once per engine
     bool bm_ready = false;
+    bool l2_limit_set = false;
     SgDev prop_table; // sg_prop_dev per property, for compiled steps
 
     SgProfiler prof;
@@ -175,6 +177,14 @@ int sg_engine_create(const sg_engine_cfg *cfg, sg_engine **out)
     auto *e = new sg_engine();
     e->device = device;
     e->sm_count = sg_sm_count(device);
+    {
+        int persist = 0, window = 0;
+        if (cudaDeviceGetAttribute(&persist, cudaDevAttrMaxPersistingL2CacheSize, device) == cudaSuccess &&
+            cudaDeviceGetAttribute(&window, cudaDevAttrMaxAccessPolicyWindowSize, device) == cudaSuccess &&
+            persist > 0 && window > 0)
+            e->l2_window_max = (size_t)std::min(persist, window);
+        (void)cudaGetLastError();
+    }
     if (cfg && cfg->stream) {
         e->stream = (cudaStream_t)cfg->stream;
     } else {
@@ -578,6 +588,8 @@ static SgTickArgs base_args(sg_engine *e, SgStep *s, int32_t r, bool inplace)
     a.mega_blocks = std::min(s->nmega, e->sm_count);
     a.mega_row = kMegaRow;
     a.cnt = e->cnt.as<int32_t>();
+    if (e->cls_on && s->bp.strategy == SG_SIR_COUNT)
+        a.cnt_window = std::min(e->l2_window_max, (size_t)e->n * sizeof(int32_t));
     a.changes = e->changes.as<int32_t>();
     a.tile_nch = e->tile_nch.as<int32_t>();
     a.chunks = e->chunks.as<SgChunk>();
@@ -790,6 +802,12 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
         SG_CK(e->mrebuild.reserve((size_t)nticks + 1));
         SG_CK(e->tick_changes.reserve((size_t)std::max(nticks, 1) * 4));
         SG_CK(e->tick_cand.reserve((size_t)std::max(nticks, 1) * 4));
+    }
+    if (e->cls_on && e->l2_window_max && !e->l2_limit_set) {
+        // persisting-line capacity of this context (ends with it) for the counts' window
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, std::min(e->l2_window_max, (size_t)e->n * 4));
+        (void)cudaGetLastError();
+        e->l2_limit_set = true;
     }
     e->last_sweep = e->cls_on && pl.count_inplace && (e->tune.count_flavour & SG_FLAVOUR_SWEEP) &&
                     ((e->tune.count_flavour & SG_FLAVOUR_FORCE) ||

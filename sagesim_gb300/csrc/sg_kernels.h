@@ -138,6 +138,8 @@ struct SgTickArgs {
     int32_t *tick_cand;     // NULL, or [ticks] candidates the sweep processed at tick r
                             // (zero before the run)
     int32_t sweep_wpt;      // class sweep: warps per tile (1, 2 or 4; see sg_sweep_wpt)
+    size_t cnt_window;      // count strategy: bytes of cnt to keep in L2 as persisting lines
+                            // (an access-policy window on the count kernels); 0 = none
     const double *bm_radius; // opinion: NULL, or the 2^23-entry Box-Muller tables of
     const double *bm_cos;    // sg_launch_opinion_tables
     int32_t hybrid_rise;    // hybrid count step (0 = off): tick r > 1 runs the loop form
