@@ -765,11 +765,19 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
         SG_CK(e->fstats_delta.reserve((size_t)std::max(nticks, 1) * 32));
     }
     {
-        // property views of compiled steps; cur0 fixes the parity at r == 0
+        // property views of compiled steps; cur0 fixes the parity at r == 0. A
+        // double-buffered property that no step of the run writes keeps its
+        // current buffer for the whole run (its other buffer is not kept up to date).
         std::vector<sg_prop_dev> tab;
-        for (auto &p : e->props)
-            tab.push_back(sg_prop_dev{p->buf[0].p, p->dbuf ? p->buf[1].p : p->buf[0].p, p->width,
-                                      p->dbuf ? 1 : 0, p->cur, p->dtype});
+        for (size_t k = 0; k < e->props.size(); ++k) {
+            const SgProp &p = *e->props[k];
+            const bool swaps = p.dbuf && std::find(pl.swap_props.begin(), pl.swap_props.end(), (int32_t)k) !=
+                                             pl.swap_props.end();
+            if (swaps)
+                tab.push_back(sg_prop_dev{p.buf[0].p, p.buf[1].p, p.width, 1, p.cur, p.dtype});
+            else
+                tab.push_back(sg_prop_dev{p.buf[p.cur].p, p.buf[p.cur].p, p.width, 0, 0, p.dtype});
+        }
         SG_CK(e->prop_table.reserve(std::max<size_t>(tab.size(), 1) * sizeof(sg_prop_dev)));
         if (!tab.empty())
             SG_CK(cudaMemcpyAsync(e->prop_table.p, tab.data(), tab.size() * sizeof(sg_prop_dev),

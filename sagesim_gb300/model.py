@@ -22,7 +22,7 @@ from . import _native as N
 from .agent import AgentFactory
 from .breed import Breed  # noqa: F401  (re-exported for drop-in imports)
 from .engine import Engine
-from .steps import CudaStep, OpinionStep, SIRStep
+from .steps import CudaStep, OpinionStep, PythonStep, SIRStep
 
 
 class Model:
@@ -141,11 +141,9 @@ class Model:
         steps = []  # (priority, breed_idx, step, module_path)
         for breed in af.breeds:
             for priority, (fn, path) in breed.step_funcs.items():
-                if not isinstance(fn, (SIRStep, OpinionStep, CudaStep)):
-                    raise TypeError(
-                        "step function %r of breed %s is not a SIRStep, OpinionStep or CudaStep; "
-                        "CuPy-JIT Python step functions are written as CUDA C++ here (CudaStep)"
-                        % (fn, breed.name))
+                if not isinstance(fn, (SIRStep, OpinionStep, CudaStep, PythonStep)):
+                    # SAGESim's own Python step function: translated at setup
+                    fn = PythonStep(fn, path)
                 steps.append((priority, breed._breedidx, fn, path))
         steps.sort(key=lambda s: (s[0], s[1]))
         self._steps = steps
@@ -239,6 +237,11 @@ class Model:
         self._goffs = goffs
         e.set_globals(gflat)
         self._globals_dirty = False
+        # Python-dialect steps: globals and properties mapped by position
+        gnames = [k for k, _ in sorted(self._global_names.items(), key=lambda kv: kv[1])]
+        pdt = {k: ("i" if v[0] == np.int32 else "f") for k, v in self._props.items()}
+        self._steps = [(pr, bi, (fn.translate(gnames, list(self._props), pdt) if isinstance(fn, PythonStep) else fn),
+                        path) for pr, bi, fn, path in self._steps]
         self._pid = {}
         for name, (dt, width, arr) in self._props.items():
             self._pid[name] = e.add_property(name, dt, width, init=arr,

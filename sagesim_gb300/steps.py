@@ -14,6 +14,10 @@ tests/test_simulation.py:24-43). Here a step is one of:
                sg_ctx API of include/sagesim_gb300_step.h, compiled with NVRTC
                into the tick kernel. Property and global indices are available
                as PROP_<name> and G_<name> macros.
+  PythonStep   a step function in SAGESim's own Python dialect (a CuPy-JIT
+               rawkernel or a plain function), translated to a CudaStep at
+               setup (sagesim_gb300/translate.py). Any other object passed to
+               register_step_func is taken as such a function.
 
 Globals are referred to by the names given to Model.register_global_property,
 as the reference passes them positionally by registration order
@@ -70,3 +74,32 @@ class CudaStep:
     @property
     def writes(self):
         return self._writes
+
+
+class PythonStep:
+    """A step function in SAGESim's Python dialect, read from its module file
+    (the path given to register_step_func) and translated to CUDA C++ when the
+    model is set up, with the model's globals and properties mapped by position
+    as the reference passes them."""
+
+    def __init__(self, step_func, module_fpath=None):
+        from .translate import find_step_source
+
+        self.source, self.name = find_step_source(step_func, module_fpath)
+        self._writes = None
+
+    def translate(self, globals_, props, prop_dtypes):
+        from .translate import translate_step
+
+        src, entry, writes = translate_step(self.source, self.name, globals_, props, prop_dtypes)
+        self._writes = tuple(writes)
+        return CudaStep(src, entry, writes=list(writes))
+
+    @property
+    def writes(self):
+        if self._writes is None:
+            raise RuntimeError("PythonStep %s is translated at setup" % self.name)
+        return self._writes
+
+    def __repr__(self):
+        return "PythonStep(%r)" % self.name

@@ -1,0 +1,501 @@
+"""Translator from SAGESim's Python step dialect to a CUDA C++ step.
+
+SAGESim step functions are CuPy-JIT Python (`@jit.rawkernel(device="cuda")`)
+with the signature
+
+    step(tick, agent_index, <globals...>, agent_ids, breeds, locations, <properties...>)
+
+(the call the reference generates, sagesim/model.py:2312-2330: globals in
+registration order, then the agent ids, then every property in property order,
+starting with the breed and the neighbour rows). The reference rewrites the body
+before compiling it: neighbour rows become CSR reads (`_CSRBodyTransformer`,
+sagesim/model.py:1643-1902), the seed and the agent's logical id are injected into
+`rand_uniform_philox` / `rand_normal` (`_inject_seed`, model.py:1903-1953), and
+property writes go to the write buffer (model.py:2085-2222). This module applies
+the same meaning while emitting C++ for `sg_compile_step`, whose `sg_ctx` already
+implements those three rewrites (reads from the read buffer, writes to the write
+buffer, `ctx.rand_uniform(i, salt)` with seed and logical id filled in).
+
+Supported subset (what the reference's own step functions use): assignments and
+augmented assignments to locals and to property elements, `if` / `elif` / `else`,
+`while`, `for ... in range(...)`, `break`, `continue`, bare `return`; arithmetic,
+comparisons, `and` / `or` / `not`; `int()`, `float()`, `bool()`, `abs()`, `min()`,
+`max()`, `len(row)`, `cp.float32()`, `cp.float64()`, `cp.int32()`, `cp.isnan()`,
+`math` / `cp` `exp log sqrt sin cos tan tanh floor ceil fabs`;
+`rand_uniform_philox(tick, agent, salt)` and `rand_normal(tick, agent, salt)`;
+`locations[a]` (a neighbour row), `row[k]`, `len(row)`; property reads `p[a]`,
+`p[a][c]`, writes `p[a] = v`, `p[a][c] = v`; globals `g` and `g[k]`.
+
+Types follow numpy's scalar rules as CuPy-JIT does: Python int and float
+locals are int64 and float64, `cp.float32(...)` values are float32, a float32 with
+an int64 or float64 operand becomes float64, Python number literals take the other
+operand's type, `/` is true division. Integer `//` and `%` keep Python's flooring
+semantics. Anything outside the subset raises `StepTranslationError` naming the
+line.
+"""
+import ast
+import inspect
+import os
+import textwrap
+
+__all__ = ["StepTranslationError", "translate_step", "find_step_source"]
+
+
+class StepTranslationError(ValueError):
+    pass
+
+
+# types: "i" int64, "f" float32, "d" float64, "b" bool, "row" neighbour row,
+# "wi" / "wf" weak (literal) int / float
+_CT = {"i": "long long", "f": "float", "d": "double", "b": "bool"}
+_MATH = {"exp", "log", "sqrt", "sin", "cos", "tan", "tanh", "floor", "ceil", "fabs", "log10", "log2"}
+_PRELUDE = r"""
+__device__ __forceinline__ long long sg_py_floordiv(long long a, long long b)
+{
+    long long q = a / b;
+    if ((a % b != 0) && ((a < 0) != (b < 0))) --q;
+    return q;
+}
+__device__ __forceinline__ long long sg_py_mod(long long a, long long b)
+{
+    long long m = a % b;
+    if (m != 0 && ((m < 0) != (b < 0))) m += b;
+    return m;
+}
+"""
+
+
+def find_step_source(step_func, module_fpath=None):
+    """(source of the module, function name) for a step function: its module file
+    (the path given to register_step_func, as the reference reads it) or, for a plain
+    Python function, inspect.getsource. A CuPy-JIT rawkernel object needs no CuPy
+    here: only its __name__ and the module path are used."""
+    name = getattr(step_func, "__name__", None) or getattr(getattr(step_func, "_func", None), "__name__", None)
+    if name is None:
+        raise StepTranslationError("step function %r has no __name__" % (step_func,))
+    if module_fpath and os.path.isfile(str(module_fpath)):
+        with open(module_fpath) as f:
+            return f.read(), name
+    try:
+        return textwrap.dedent(inspect.getsource(step_func)), name
+    except (OSError, TypeError) as exc:
+        raise StepTranslationError("cannot read the source of %s: %s" % (name, exc))
+
+
+def _promote(a, b):
+    if a == "row" or b == "row":
+        raise TypeError("a neighbour row is not a number")
+    a = "i" if a == "b" else a
+    b = "i" if b == "b" else b
+    strong = [t for t in (a, b) if t in ("i", "f", "d")]
+    if not strong:
+        return "d" if "wf" in (a, b) else "i"
+    if len(strong) == 1:
+        s, w = strong[0], (b if a == strong[0] else a)
+        if s == "i" and w == "wf":
+            return "d"
+        return s
+    if a == b:
+        return a
+    return "d"  # f with i, f with d, i with d
+
+
+class _Translator:
+    def __init__(self, fn, globals_, props, prop_dtypes, entry):
+        self.fn = fn
+        self.entry = entry
+        args = [a.arg for a in fn.args.args]
+        ng = len(globals_)
+        if len(args) < 2 + ng + 1:
+            raise StepTranslationError("%s: expected (tick, agent_index, %d globals, agent_ids, breeds, "
+                                       "locations, properties...), got %d parameters"
+                                       % (fn.name, ng, len(args)))
+        self.tick = args[0]
+        self.agent = args[1]
+        self.globals = dict(zip(args[2:2 + ng], globals_))
+        rest = args[2 + ng:]
+        self.agent_ids = rest[0]
+        pnames = ["breed", "locations"] + list(props)
+        self.props = {}
+        self.breeds = self.locations = None
+        for a, p in zip(rest[1:], pnames):
+            if p == "breed":
+                self.breeds = a
+            elif p == "locations":
+                self.locations = a
+            else:
+                self.props[a] = p
+        self.prop_dtypes = prop_dtypes
+        self.locals = {}  # name -> type
+        self.row_of = {}  # row local -> agent expression
+        self.writes = set()
+        self.out = []
+
+    def err(self, node, msg):
+        raise StepTranslationError("%s line %d: %s" % (self.fn.name, getattr(node, "lineno", 0), msg))
+
+    # ---- expressions ----------------------------------------------------------------
+    def expr(self, n):
+        """(C++ text, type) of an expression."""
+        if isinstance(n, ast.Constant):
+            v = n.value
+            if isinstance(v, bool):
+                return ("true" if v else "false"), "b"
+            if isinstance(v, int):
+                return ("%dLL" % v), "wi"
+            if isinstance(v, float):
+                return repr(v) if "e" in repr(v) or "." in repr(v) else repr(v) + ".0", "wf"
+            self.err(n, "unsupported constant %r" % (v,))
+        if isinstance(n, ast.Name):
+            if n.id == self.tick:
+                return "ctx.tick", "i"
+            if n.id == self.agent:
+                return "sg_agent", "i"
+            if n.id in self.globals:
+                return "ctx.g[G_%s]" % self.globals[n.id], "d"
+            if n.id in ("True", "False"):
+                return n.id.lower(), "b"
+            if n.id in self.row_of:
+                return self.row_of[n.id], "row"
+            if n.id in self.locals:
+                return "u_" + n.id, self.locals[n.id]
+            self.err(n, "unknown name %r" % n.id)
+        if isinstance(n, ast.BinOp):
+            return self.binop(n)
+        if isinstance(n, ast.UnaryOp):
+            s, t = self.expr(n.operand)
+            if isinstance(n.op, ast.Not):
+                return "(!(%s))" % s, "b"
+            if isinstance(n.op, ast.USub):
+                return "(-(%s))" % s, ("i" if t == "b" else t)
+            if isinstance(n.op, ast.UAdd):
+                return s, t
+            self.err(n, "unsupported unary operator")
+        if isinstance(n, ast.BoolOp):
+            op = " && " if isinstance(n.op, ast.And) else " || "
+            return "(" + op.join("(%s)" % self.expr(v)[0] for v in n.values) + ")", "b"
+        if isinstance(n, ast.Compare):
+            parts = []
+            left, lt = self.expr(n.left)
+            for op, comp in zip(n.ops, n.comparators):
+                right, rt = self.expr(comp)
+                sym = {ast.Lt: "<", ast.LtE: "<=", ast.Gt: ">", ast.GtE: ">=", ast.Eq: "==",
+                       ast.NotEq: "!="}.get(type(op))
+                if sym is None:
+                    self.err(n, "unsupported comparison")
+                parts.append("((%s) %s (%s))" % (left, sym, right))
+                left = right
+            return "(" + " && ".join(parts) + ")", "b"
+        if isinstance(n, ast.IfExp):
+            c, _ = self.expr(n.test)
+            a, at = self.expr(n.body)
+            b, bt = self.expr(n.orelse)
+            t = _promote(at, bt)
+            t = "i" if t == "wi" else ("d" if t == "wf" else t)
+            return "((%s) ? (%s)(%s) : (%s)(%s))" % (c, _CT[t], a, _CT[t], b), t
+        if isinstance(n, ast.Subscript):
+            return self.subscript(n)
+        if isinstance(n, ast.Call):
+            return self.call(n)
+        self.err(n, "unsupported expression %s" % type(n).__name__)
+
+    def binop(self, n):
+        a, at = self.expr(n.left)
+        b, bt = self.expr(n.right)
+        op = n.op
+        if isinstance(op, ast.Div):
+            t = _promote(at, bt)
+            t = "d" if t in ("i", "wi", "wf") else t
+            return "((%s)(%s) / (%s)(%s))" % (_CT[t], a, _CT[t], b), t
+        t = _promote(at, bt)
+        if isinstance(op, (ast.FloorDiv, ast.Mod)):
+            if t in ("i", "wi"):
+                f = "sg_py_floordiv" if isinstance(op, ast.FloorDiv) else "sg_py_mod"
+                return "%s((long long)(%s), (long long)(%s))" % (f, a, b), "i"
+            if isinstance(op, ast.FloorDiv):
+                t = "d" if t == "wf" else t
+                return "floor((%s)(%s) / (%s)(%s))" % (_CT[t], a, _CT[t], b), t
+            self.err(n, "float %% is not supported")
+        if isinstance(op, ast.Pow):
+            return "pow((double)(%s), (double)(%s))" % (a, b), "d"
+        sym = {ast.Add: "+", ast.Sub: "-", ast.Mult: "*", ast.BitAnd: "&", ast.BitOr: "|",
+               ast.BitXor: "^", ast.LShift: "<<", ast.RShift: ">>"}.get(type(op))
+        if sym is None:
+            self.err(n, "unsupported operator %s" % type(op).__name__)
+        if t in ("wi", "wf"):
+            return "((%s) %s (%s))" % (a, sym, b), t
+        return "((%s)(%s) %s (%s)(%s))" % (_CT[t], a, sym, _CT[t], b), t
+
+    def prop_read(self, node, pname, agent, comp=None):
+        dt = self.prop_dtypes[pname]
+        fn = "i32" if dt == "i" else "f32"
+        if comp is None:
+            return "ctx.%s(PROP_%s, (int)(%s))" % (fn, pname, agent), ("i" if dt == "i" else "f")
+        return "ctx.%s(PROP_%s, (int)(%s), (int)(%s))" % (fn, pname, agent, comp), ("i" if dt == "i" else "f")
+
+    def subscript(self, n):
+        base, idx = n.value, n.slice
+        # p[a][c]
+        if isinstance(base, ast.Subscript) and isinstance(base.value, ast.Name) and base.value.id in self.props:
+            a, _ = self.expr(base.slice)
+            c, _ = self.expr(idx)
+            return self.prop_read(n, self.props[base.value.id], a, c)
+        if isinstance(base, ast.Name):
+            if base.id in self.props:
+                if isinstance(idx, ast.Tuple) and len(idx.elts) == 2:
+                    a, _ = self.expr(idx.elts[0])
+                    c, _ = self.expr(idx.elts[1])
+                    return self.prop_read(n, self.props[base.id], a, c)
+                a, _ = self.expr(idx)
+                return self.prop_read(n, self.props[base.id], a)
+            if base.id == self.locations:
+                a, _ = self.expr(idx)
+                return a, "row"
+            if base.id in self.globals:
+                k, _ = self.expr(idx)
+                return "ctx.g[G_%s + (int)(%s)]" % (self.globals[base.id], k), "d"
+            if base.id in self.row_of:
+                k, _ = self.expr(idx)
+                return "(long long)ctx.neighbor((int)(%s), (int)(%s))" % (self.row_of[base.id], k), "i"
+        if isinstance(base, ast.Subscript) and isinstance(base.value, ast.Name) and base.value.id == self.locations:
+            a, _ = self.expr(base.slice)
+            k, _ = self.expr(idx)
+            return "(long long)ctx.neighbor((int)(%s), (int)(%s))" % (a, k), "i"
+        self.err(n, "unsupported subscript")
+
+    def call(self, n):
+        f = n.func
+        name = f.id if isinstance(f, ast.Name) else (f.attr if isinstance(f, ast.Attribute) else None)
+        mod = f.value.id if isinstance(f, ast.Attribute) and isinstance(f.value, ast.Name) else None
+        args = n.args
+        if name in ("rand_uniform_philox", "rand_normal"):
+            if len(args) != 3:
+                self.err(n, "%s takes (tick, agent, salt)" % name)
+            if not (isinstance(args[0], ast.Name) and args[0].id == self.tick):
+                self.err(n, "%s must be drawn at the current tick" % name)
+            a, _ = self.expr(args[1])
+            s, _ = self.expr(args[2])
+            m = "rand_uniform" if name == "rand_uniform_philox" else "rand_normal"
+            return "ctx.%s((int)(%s), (long long)(%s))" % (m, a, s), "d"
+        if name == "len" and mod is None:
+            if len(args) == 1:
+                r, t = self.expr(args[0])
+                if t == "row":
+                    return "(long long)ctx.degree((int)(%s))" % r, "i"
+            self.err(n, "len() of a neighbour row only")
+        if name == "isnan":
+            a0 = args[0]
+            if isinstance(a0, ast.Subscript) and self._is_row_element(a0):
+                return "false", "b"  # CSR rows hold no padding
+            s, _ = self.expr(a0)
+            return "isnan((double)(%s))" % s, "b"
+        if name in ("int", "int32", "int64") and (mod in (None, "cp", "np", "numpy", "cupy")):
+            s, _ = self.expr(args[0])
+            return "(long long)(%s)" % s, "i"
+        if name in ("float", "float64") and (mod in (None, "cp", "np", "numpy", "cupy")):
+            s, _ = self.expr(args[0])
+            return "(double)(%s)" % s, "d"
+        if name == "float32" and mod in ("cp", "np", "numpy", "cupy"):
+            s, _ = self.expr(args[0])
+            return "(float)(%s)" % s, "f"
+        if name == "bool" and mod is None:
+            s, _ = self.expr(args[0])
+            return "((bool)(%s))" % s, "b"
+        if name == "abs" and mod is None or name == "fabs":
+            s, t = self.expr(args[0])
+            if t in ("f",):
+                return "fabsf(%s)" % s, "f"
+            if t in ("i", "wi", "b"):
+                return "llabs((long long)(%s))" % s, "i"
+            return "fabs((double)(%s))" % s, "d"
+        if name in ("min", "max") and mod is None:
+            if len(args) != 2:
+                self.err(n, "min/max of two values only")
+            a, at = self.expr(args[0])
+            b, bt = self.expr(args[1])
+            t = _promote(at, bt)
+            t = "i" if t == "wi" else ("d" if t == "wf" else t)
+            op = "<" if name == "min" else ">"
+            return "((%s)(%s) %s (%s)(%s) ? (%s)(%s) : (%s)(%s))" % (
+                _CT[t], a, op, _CT[t], b, _CT[t], a, _CT[t], b), t
+        if name in _MATH and mod in ("math", "cp", "np", "numpy", "cupy"):
+            s, t = self.expr(args[0])
+            if t == "f" and mod != "math":
+                return "%sf(%s)" % (name, s), "f"
+            return "%s((double)(%s))" % (name, s), "d"
+        self.err(n, "unsupported call %s" % (ast.unparse(f) if hasattr(ast, "unparse") else name))
+
+    def _is_row_element(self, n):
+        b = n.value
+        if isinstance(b, ast.Name) and b.id in self.row_of:
+            return True
+        return isinstance(b, ast.Subscript) and isinstance(b.value, ast.Name) and b.value.id == self.locations
+
+    # ---- statements ------------------------------------------------------------------
+    def declare(self, name, t, node):
+        t = "i" if t == "wi" else ("d" if t == "wf" else t)
+        if name in (self.tick, self.agent) or name in self.globals or name in self.props:
+            self.err(node, "cannot assign to parameter %r" % name)
+        old = self.locals.get(name)
+        if old is None:
+            self.locals[name] = t
+        elif old != t and "row" not in (old, t):
+            # numpy rebinding: keep the wider type for the C++ declaration
+            self.locals[name] = "d" if "d" in (old, t) else ("f" if "f" in (old, t) else old)
+
+    def scan(self, body):
+        """First pass: local variable types (assignments in program order)."""
+        for s in body:
+            for node in ast.walk(s):
+                if isinstance(node, ast.Assign) and len(node.targets) == 1 and isinstance(node.targets[0], ast.Name):
+                    name = node.targets[0].id
+                    v = node.value
+                    if isinstance(v, ast.Subscript) and isinstance(v.value, ast.Name) and v.value.id == self.locations:
+                        self.locals[name] = "row"
+                        self.row_of[name] = self.expr(v.slice)[0]
+                        continue
+                    try:
+                        _, t = self.expr(v)
+                    except StepTranslationError:
+                        continue  # depends on a local not typed yet; second pass below
+                    self.declare(name, t, node)
+                elif isinstance(node, ast.For) and isinstance(node.target, ast.Name):
+                    self.declare(node.target.id, "i", node)
+        # second pass for assignments that referenced later-typed locals
+        for s in body:
+            for node in ast.walk(s):
+                if isinstance(node, ast.Assign) and len(node.targets) == 1 and isinstance(node.targets[0], ast.Name):
+                    name = node.targets[0].id
+                    if name not in self.locals:
+                        _, t = self.expr(node.value)
+                        self.declare(name, t, node)
+
+    def emit(self, line, depth):
+        self.out.append("    " * depth + line)
+
+    def block(self, body, depth):
+        for s in body:
+            self.stmt(s, depth)
+
+    def stmt(self, s, d):
+        if isinstance(s, ast.Expr):
+            if isinstance(s.value, ast.Constant) and isinstance(s.value.value, str):
+                return  # docstring
+            self.err(s, "expression statements are not supported")
+        if isinstance(s, ast.Pass):
+            return
+        if isinstance(s, ast.Assign):
+            if len(s.targets) != 1:
+                self.err(s, "one assignment target only")
+            return self.assign(s.targets[0], s.value, d, s)
+        if isinstance(s, ast.AugAssign):
+            tgt = s.target
+            val = ast.BinOp(left=_load(tgt), op=s.op, right=s.value)
+            ast.copy_location(val, s)
+            return self.assign(tgt, val, d, s)
+        if isinstance(s, ast.If):
+            c, _ = self.expr(s.test)
+            self.emit("if (%s) {" % c, d)
+            self.block(s.body, d + 1)
+            if s.orelse:
+                self.emit("} else {", d)
+                self.block(s.orelse, d + 1)
+            self.emit("}", d)
+            return
+        if isinstance(s, ast.While):
+            if s.orelse:
+                self.err(s, "while ... else is not supported")
+            c, _ = self.expr(s.test)
+            self.emit("while (%s) {" % c, d)
+            self.block(s.body, d + 1)
+            self.emit("}", d)
+            return
+        if isinstance(s, ast.For):
+            it = s.iter
+            if not (isinstance(it, ast.Call) and isinstance(it.func, ast.Name) and it.func.id == "range"
+                    and isinstance(s.target, ast.Name) and not s.orelse):
+                self.err(s, "for loops over range() only")
+            a = [self.expr(x)[0] for x in it.args]
+            lo, hi, st = ("0LL", a[0], "1LL") if len(a) == 1 else (a[0], a[1], a[2] if len(a) == 3 else "1LL")
+            v = "u_" + s.target.id
+            self.emit("for (%s = (long long)(%s); ((long long)(%s) > 0) ? (%s < (long long)(%s)) : "
+                      "(%s > (long long)(%s)); %s += (long long)(%s)) {" % (v, lo, st, v, hi, v, hi, v, st), d)
+            self.block(s.body, d + 1)
+            self.emit("}", d)
+            return
+        if isinstance(s, ast.Break):
+            return self.emit("break;", d)
+        if isinstance(s, ast.Continue):
+            return self.emit("continue;", d)
+        if isinstance(s, ast.Return):
+            if s.value is not None:
+                self.err(s, "a step returns nothing")
+            return self.emit("return;", d)
+        self.err(s, "unsupported statement %s" % type(s).__name__)
+
+    def assign(self, tgt, value, d, node):
+        if isinstance(tgt, ast.Name):
+            if self.locals.get(tgt.id) == "row":
+                return  # declared as a row alias; nothing to emit
+            v, _ = self.expr(value)
+            t = self.locals[tgt.id]
+            return self.emit("u_%s = (%s)(%s);" % (tgt.id, _CT[t], v), d)
+        if isinstance(tgt, ast.Subscript):
+            base, idx = tgt.value, tgt.slice
+            comp = None
+            if isinstance(base, ast.Subscript) and isinstance(base.value, ast.Name) and base.value.id in self.props:
+                pname = self.props[base.value.id]
+                agent, _ = self.expr(base.slice)
+                comp, _ = self.expr(idx)
+            elif isinstance(base, ast.Name) and base.id in self.props:
+                pname = self.props[base.id]
+                if isinstance(idx, ast.Tuple) and len(idx.elts) == 2:
+                    agent, _ = self.expr(idx.elts[0])
+                    comp, _ = self.expr(idx.elts[1])
+                else:
+                    agent, _ = self.expr(idx)
+            else:
+                self.err(node, "assignment to a subscript of a property only")
+            v, _ = self.expr(value)
+            self.writes.add(pname)
+            fn = "set_i32" if self.prop_dtypes[pname] == "i" else "set_f32"
+            cast = "int" if self.prop_dtypes[pname] == "i" else "float"
+            if comp is None:
+                return self.emit("ctx.%s(PROP_%s, (int)(%s), (%s)(%s));" % (fn, pname, agent, cast, v), d)
+            return self.emit("ctx.%s(PROP_%s, (int)(%s), (%s)(%s), (int)(%s));" % (fn, pname, agent, cast, v, comp), d)
+        self.err(node, "unsupported assignment target")
+
+    def run(self):
+        self.scan(self.fn.body)
+        decls = ["    %s u_%s = 0;" % (_CT[t], name) for name, t in self.locals.items() if t != "row"]
+        self.block(self.fn.body, 1)
+        src = [_PRELUDE, "__device__ void %s(const sg_ctx &ctx, int sg_agent)" % self.entry, "{"]
+        src += decls
+        src += self.out
+        src.append("}")
+        return "\n".join(src)
+
+
+def _load(t):
+    n = ast.parse(ast.unparse(t), mode="eval").body if hasattr(ast, "unparse") else t
+    return n
+
+
+def translate_step(source, name, globals_, props, prop_dtypes, entry=None):
+    """CUDA C++ for step `name` defined in `source`.
+
+    globals_: the model's global property names in registration order.
+    props: the model's agent property names in property order (without the
+    breed and the neighbour rows). prop_dtypes: name -> "i" (int32) or "f"
+    (float32). Returns (C++ source, entry name, properties written)."""
+    tree = ast.parse(source)
+    fn = None
+    for node in ast.walk(tree):
+        if isinstance(node, ast.FunctionDef) and node.name == name:
+            fn = node
+            break
+    if fn is None:
+        raise StepTranslationError("no function %r in the step's source" % name)
+    entry = entry or ("sg_py_" + name)
+    tr = _Translator(fn, list(globals_), list(props), dict(prop_dtypes), entry)
+    return tr.run(), entry, sorted(tr.writes)

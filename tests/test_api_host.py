@@ -107,12 +107,20 @@ def test_model_lifecycle_host():
         m.register_breed(Breed("Late"))
 
 
-def test_python_step_function_rejected_with_clear_message():
+def test_python_step_function_is_taken_as_reference_dialect():
+    """A plain function is a step in SAGESim's Python dialect, translated at setup;
+    one whose source cannot be found fails with the translator's message."""
+    from sagesim_gb300.steps import PythonStep
+    from sagesim_gb300.translate import StepTranslationError
+
     m, _ = make_space(2)
     b = list(m._agent_factory.breeds)[0]
     b.register_step_func(lambda *a: None, __file__, priority=0)
-    with pytest.raises(TypeError, match="CudaStep"):
-        m._collect_steps()
+    m._collect_steps()
+    step = m._steps[0][2]
+    assert isinstance(step, PythonStep)
+    with pytest.raises(StepTranslationError, match="no function"):
+        step.translate([], ["state"], {"state": "i"})
 
 
 def test_host_arrays_breed_sort_csr_and_logical_ids():

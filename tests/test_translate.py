@@ -1,0 +1,93 @@
+"""The Python step-dialect translator on the host: output shape, typing rules
+and refusals (compilation and results are checked on the GPU in
+test_model_gpu.py)."""
+import os
+
+import pytest
+
+from sagesim_gb300.translate import StepTranslationError, translate_step
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _tr(src, name="step", globals_=("p",), props=("state",), dtypes=None):
+    return translate_step(src, name, list(globals_), list(props), dtypes or {"state": "i"})
+
+
+def test_reference_dialect_steps_translate():
+    src = open(os.path.join(GOLD, "ref_steps.py")).read()
+    code, entry, writes = translate_step(src, "sir_per_neighbour_step", ["p_infection", "p_recovery"],
+                                         ["state"], {"state": "i"})
+    assert entry == "sg_py_sir_per_neighbour_step" and writes == ["state"]
+    assert "ctx.degree((int)(sg_agent))" in code
+    assert "ctx.rand_uniform((int)(sg_agent), (long long)(((long long)(2LL) + (long long)(u_j))))" in code
+    assert "ctx.g[G_p_recovery]" in code
+    code, _, writes = translate_step(src, "opinion_step", ["noise_sigma"], ["opinion", "weights"],
+                                     {"opinion": "f", "weights": "f"})
+    assert writes == ["opinion"]
+    assert "float u_acc" in code and "double u_y" in code
+    assert "ctx.f32(PROP_weights, (int)(sg_agent), (int)(u_j))" in code
+    assert "ctx.rand_normal((int)(sg_agent), (long long)(1LL))" in code
+
+
+def test_numpy_typing_rules():
+    src = '''
+def step(tick, agent_index, p, agent_ids, breeds, locations, state):
+    a = 3
+    b = a / 2
+    c = a // 2
+    d = cp.float32(1.5)
+    e = d * 2.0
+    f = d * a
+    g = -7 % 3
+'''
+    code, _, _ = _tr(src)
+    assert "long long u_a" in code
+    assert "double u_b" in code and "((double)(u_a) / (double)(2LL))" in code
+    assert "long long u_c" in code and "sg_py_floordiv" in code
+    assert "float u_d" in code
+    assert "float u_e" in code  # a float32 with a literal stays float32
+    assert "double u_f" in code  # float32 with int64 becomes float64
+    assert "sg_py_mod" in code
+
+
+def test_loops_and_property_components():
+    src = '''
+def step(tick, agent_index, p, agent_ids, breeds, locations, state, weights):
+    row = locations[agent_index]
+    total = 0.0
+    for k in range(len(row)):
+        if cp.isnan(row[k]):
+            break
+        total += weights[agent_index][k] * p
+    weights[agent_index, 0] = total
+    if total > 1.0:
+        return
+'''
+    code, _, writes = _tr(src, props=("state", "weights"), dtypes={"state": "i", "weights": "f"})
+    assert writes == ["weights"]
+    assert "for (u_k = (long long)(0LL);" in code
+    assert "if (false)" in code  # CSR rows carry no NaN padding
+    assert "ctx.set_f32(PROP_weights, (int)(sg_agent), (float)(u_total), (int)(0LL));" in code
+    assert "return;" in code
+
+
+@pytest.mark.parametrize("body,msg", [
+    ("    x = [1, 2]\n", "unsupported expression"),
+    ("    foo(1)\n", "expression statements"),
+    ("    y = rand_uniform_philox(tick + 1, agent_index, 1)\n", "current tick"),
+    ("    tick = 3\n", "cannot assign to parameter"),
+    ("    for k in items:\n        pass\n", "range()"),
+    ("    return 1\n", "returns nothing"),
+])
+def test_refusals_name_the_line(body, msg):
+    src = "def step(tick, agent_index, p, agent_ids, breeds, locations, state):\n" + body
+    with pytest.raises(StepTranslationError, match=msg):
+        _tr(src)
+
+
+def test_missing_function_and_short_signature():
+    with pytest.raises(StepTranslationError, match="no function"):
+        _tr("def other(tick, agent_index):\n    pass\n")
+    with pytest.raises(StepTranslationError, match="expected"):
+        _tr("def step(tick, agent_index):\n    pass\n", globals_=("a", "b"))
