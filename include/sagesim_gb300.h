@@ -160,6 +160,21 @@ int sg_last_error(const sg_engine *e, char *buf, size_t cap);
  * graph and fixes the agent count n. */
 int sg_set_graph_csr(sg_engine *e, const int32_t *offsets, int64_t n, const int32_t *indices,
                      int64_t nnz, int32_t flags);
+/* Graph from an edge list in agent ids, built on the GPU (replaces the
+ * reference's id -> index conversion, sagesim/model.py:31-110, and its host CSR
+ * build, sagesim/internal_utils.py:111-186, for NetworkSpace.connect_agents
+ * graphs). ids[0..n): each agent's id in buffer order (distinct, any int64 but
+ * INT64_MIN); an open-addressing hash table in HBM maps ids to buffer indices.
+ * (src_ids[k], dst_ids[k]), k < nedges: host arrays of edges. flags:
+ * SG_GRAPH_SYMMETRIC adds each edge in both directions; SG_GRAPH_ORDERED keeps
+ * a row in first-connection order (NetworkSpace(ordered=True)), else rows are
+ * sorted by neighbour index. Repeated edges are dropped. A repeated id is
+ * SG_ERR_INVALID, an edge naming an unknown id SG_ERR_BAD_CSR. */
+int sg_set_graph_id_edges(sg_engine *e, const int64_t *ids, int64_t n, const int64_t *src_ids,
+                          const int64_t *dst_ids, int64_t nedges, int32_t flags);
+/* Copies the engine's CSR to host arrays (offsets: n + 1, indices: nnz; either
+ * may be NULL) and returns nnz. */
+int sg_get_graph_csr(sg_engine *e, int32_t *offsets, int32_t *indices, int64_t *nnz);
 /* RNG key per agent (default: the agent index). */
 int sg_set_logical_ids(sg_engine *e, const int64_t *lids, int64_t n);
 int sg_set_seed(sg_engine *e, int64_t seed);

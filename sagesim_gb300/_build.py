@@ -21,8 +21,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-Wall", "-I" + BUILD, "-I" + CSRC,
          "-I" + INCLUDE]
 SOURCES = ["sg_kernels.cu", "sg_count.cu", "sg_engine.cu", "sg_batch.cu", "sg_server.cpp", "sg_step_rt.cpp",
-           "sg_graphs.cpp", "sg_noalloc.cu"]
-HEADERS = ["sg_kernels.h", "sg_device.cuh", "sg_internal.h", "sg_philox.h", "sg_step_rt.h", "sg_batch.h"]
+           "sg_graphs.cpp", "sg_noalloc.cu", "sg_setup.cu"]
+HEADERS = ["sg_kernels.h", "sg_device.cuh", "sg_setup.h", "sg_internal.h", "sg_philox.h", "sg_step_rt.h", "sg_batch.h"]
 
 
 def _nvcc():

@@ -109,6 +109,8 @@ SIGNATURES = {
     "sg_engine_destroy": [_P],
     "sg_last_error": [_P, ctypes.c_char_p, _SZ],
     "sg_set_graph_csr": [_P, _P, _I64, _P, _I64, _I32],
+    "sg_set_graph_id_edges": [_P, _P, _I64, _P, _P, _I64, _I32],
+    "sg_get_graph_csr": [_P, _P, _P, _P],
     "sg_set_logical_ids": [_P, _P, _I64],
     "sg_set_seed": [_P, _I64],
     "sg_set_globals_f64": [_P, _P, _I32],

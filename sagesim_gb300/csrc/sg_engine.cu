@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "sg_internal.h"
+#include "sg_setup.h"
 #include "sg_philox.h"
 #include "sg_step_rt.h"
 
@@ -250,6 +251,61 @@ int sg_set_graph_csr(sg_engine *e, const int32_t *offsets, int64_t n, const int3
     e->graph_flags = flags;
     e->have_transpose = false;
     e->version++;
+    return SG_OK;
+}
+
+int sg_set_graph_id_edges(sg_engine *e, const int64_t *ids, int64_t n, const int64_t *src_ids,
+                          const int64_t *dst_ids, int64_t nedges, int32_t flags)
+{
+    if (!e || (n > 0 && !ids) || (nedges > 0 && (!src_ids || !dst_ids))) return SG_ERR_INVALID;
+    if (e->n >= 0 && e->n != n && !e->props.empty())
+        return e->fail(SG_ERR_INVALID, "agent count differs from the existing properties");
+    cudaSetDevice(e->device);
+    int32_t *off = nullptr, *idx = nullptr;
+    int64_t nnz = 0;
+    std::string why;
+    const int rc = sg_build_csr_from_ids(ids, n, src_ids, dst_ids, nedges, (flags & SG_GRAPH_SYMMETRIC) != 0,
+                                         (flags & SG_GRAPH_ORDERED) != 0, e->stream, &off, &idx, &nnz, &why);
+    if (rc != SG_OK) {
+        if (off) cudaFree(off);
+        if (idx) cudaFree(idx);
+        return e->fail(rc, why);
+    }
+    if (nnz >= ((int64_t)1 << 31)) {
+        cudaFree(off);
+        cudaFree(idx);
+        return e->fail(SG_ERR_INVALID, "more than 2^31 - 1 CSR entries");
+    }
+    e->off.release();
+    e->idx.release();
+    e->off.p = off;
+    e->off.bytes = (size_t)(n + 1) * 4;
+    e->idx.p = idx;
+    e->idx.bytes = (size_t)std::max<int64_t>(nnz, 1) * 4;
+    // long rows (mega agents) from the offsets
+    std::vector<int32_t> hoff((size_t)n + 1);
+    SG_CK(cudaMemcpy(hoff.data(), off, (size_t)(n + 1) * 4, cudaMemcpyDeviceToHost));
+    e->mega_agents.clear();
+    for (int64_t i = 0; i < n; ++i)
+        if (hoff[(size_t)i + 1] - hoff[(size_t)i] > kMegaRow) e->mega_agents.push_back((int32_t)i);
+    for (auto &st : e->steps) st->ntiles = 0; // tile and mega tables are rebuilt
+    e->n = n;
+    e->nnz = nnz;
+    e->graph_flags = flags & (SG_GRAPH_SYMMETRIC | SG_GRAPH_ORDERED);
+    e->have_transpose = false;
+    e->version++;
+    return SG_OK;
+}
+
+int sg_get_graph_csr(sg_engine *e, int32_t *offsets, int32_t *indices, int64_t *nnz)
+{
+    if (!e || !nnz) return SG_ERR_INVALID;
+    if (e->n < 0) return e->fail(SG_ERR_INVALID, "no graph");
+    cudaSetDevice(e->device);
+    SG_CK(cudaStreamSynchronize(e->stream));
+    if (offsets) SG_CK(cudaMemcpy(offsets, e->off.p, (size_t)(e->n + 1) * 4, cudaMemcpyDeviceToHost));
+    if (indices && e->nnz > 0) SG_CK(cudaMemcpy(indices, e->idx.p, (size_t)e->nnz * 4, cudaMemcpyDeviceToHost));
+    *nnz = e->nnz;
     return SG_OK;
 }
 

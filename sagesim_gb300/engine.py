@@ -60,6 +60,31 @@ class Engine:
                                             idx.size, flags))
         self.n = n
 
+    def set_graph_from_ids(self, ids, src_ids, dst_ids, symmetric=True, ordered=False):
+        """Graph from an edge list in agent ids, built on the GPU: ids[k] is the id of
+        the agent at buffer index k; an HBM hash table maps the edges' ids to indices.
+        symmetric adds both directions; ordered keeps rows in first-connection order
+        (else sorted); repeated edges are dropped."""
+        ids = np.ascontiguousarray(ids, dtype=np.int64)
+        src = np.ascontiguousarray(src_ids, dtype=np.int64)
+        dst = np.ascontiguousarray(dst_ids, dtype=np.int64)
+        if src.shape != dst.shape:
+            raise ValueError("src_ids and dst_ids differ in length")
+        flags = (N.SG_GRAPH_ORDERED if ordered else 0) | (N.SG_GRAPH_SYMMETRIC if symmetric else 0)
+        self._ck(self._lib.sg_set_graph_id_edges(self._h, _ptr(ids) if ids.size else None, ids.size,
+                                                 _ptr(src) if src.size else None, _ptr(dst) if dst.size else None,
+                                                 src.size, flags))
+        self.n = ids.size
+
+    def get_graph(self):
+        """(offsets, indices) of the engine's CSR, copied to the host."""
+        nnz = ctypes.c_int64()
+        self._ck(self._lib.sg_get_graph_csr(self._h, None, None, ctypes.byref(nnz)))
+        off = np.empty(self.n + 1, dtype=np.int32)
+        idx = np.empty(max(nnz.value, 1), dtype=np.int32)
+        self._ck(self._lib.sg_get_graph_csr(self._h, _ptr(off), _ptr(idx), ctypes.byref(nnz)))
+        return off, idx[:nnz.value]
+
     def set_logical_ids(self, lids):
         if lids is None:
             self._ck(self._lib.sg_set_logical_ids(self._h, None, self.n))

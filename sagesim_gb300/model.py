@@ -167,14 +167,18 @@ class Model:
         self._breed_ranges = {b: (int(starts[b]), int(starts[b + 1])) for b in range(nb)}
 
         space = self.get_space()
-        if any(c is None for c in space._locations) and space._csr is None:
-            raise RuntimeError("agents created in bulk need NetworkSpace.set_csr before setup()")
-        off, idx = space._rows()
-        if off.size - 1 != n:
-            raise RuntimeError("the space holds %d agents, the model %d" % (off.size - 1, n))
-        from .graphs import permute_csr
+        self._id_edges = getattr(space, "_id_edges", None)
+        if self._id_edges is not None:
+            self._csr = None  # built on the GPU from the id edge list at engine build
+        else:
+            if any(c is None for c in space._locations) and space._csr is None:
+                raise RuntimeError("agents created in bulk need NetworkSpace.set_csr or set_edges before setup()")
+            off, idx = space._rows()
+            if off.size - 1 != n:
+                raise RuntimeError("the space holds %d agents, the model %d" % (off.size - 1, n))
+            from .graphs import permute_csr
 
-        self._csr = permute_csr(off, idx, pos) if n else (off, idx)
+            self._csr = permute_csr(off, idx, pos) if n else (off, idx)
 
         lids = np.arange(n, dtype=np.int64)[order]  # agent id of each buffer slot
         if self._logical_id_map:
@@ -228,8 +232,14 @@ class Model:
         if self._engine is not None:
             self._engine.close()
         e = Engine(device=self._device)
-        off, idx = self._csr
-        e.set_graph(off, idx, ordered=self.get_space().ordered)
+        if self._csr is None:
+            src, dst, directed = self._id_edges
+            # buffer slot k holds agent id self._order[k]; the engine maps ids on the GPU
+            e.set_graph_from_ids(self._order.astype(np.int64), src, dst, symmetric=not directed,
+                                 ordered=self.get_space().ordered)
+        else:
+            off, idx = self._csr
+            e.set_graph(off, idx, ordered=self.get_space().ordered)
         if self._lids is not None:
             e.set_logical_ids(self._lids)
         e.set_seed(self._seed)

@@ -15,6 +15,7 @@ class Space:
         self._locations = []
         self._agent_factory = None
         self._csr = None
+        self._id_edges = None
 
 
 def _network_space_compute_neighbors(agent_locations):
@@ -110,6 +111,20 @@ class NetworkSpace(Space):
             raise ValueError("CSR has %d rows but the space holds %d agents"
                              % (off.size - 1, len(self._locations)))
         self._csr = (off, idx)
+
+    def set_edges(self, src_ids, dst_ids, directed=False):
+        """Installs the adjacency as an edge list in agent ids (any int64 ids the
+        model's agents carry: creation-order ids here). The CSR is built on the GPU
+        at setup: an open-addressing hash table in HBM maps ids to buffer indices
+        (the reference's convert_agent_ids_to_indices, sagesim/model.py:31-110),
+        and the rows are sorted (or kept in first-connection order for an ordered
+        space), repeated edges dropped, as connect_agents would leave them."""
+        src = np.ascontiguousarray(src_ids, dtype=np.int64)
+        dst = np.ascontiguousarray(dst_ids, dtype=np.int64)
+        if src.shape != dst.shape:
+            raise ValueError("src_ids and dst_ids differ in length")
+        self._id_edges = (src, dst, bool(directed))
+        self._csr = None
 
     def _rows(self):
         """(offsets, indices) by agent id, from the CSR or the containers."""
