@@ -232,14 +232,7 @@ class Model:
         if self._engine is not None:
             self._engine.close()
         e = Engine(device=self._device)
-        if self._csr is None:
-            src, dst, directed = self._id_edges
-            # buffer slot k holds agent id self._order[k]; the engine maps ids on the GPU
-            e.set_graph_from_ids(self._order.astype(np.int64), src, dst, symmetric=not directed,
-                                 ordered=self.get_space().ordered)
-        else:
-            off, idx = self._csr
-            e.set_graph(off, idx, ordered=self.get_space().ordered)
+        self._install_graph(e)
         if self._lids is not None:
             e.set_logical_ids(self._lids)
         e.set_seed(self._seed)
@@ -286,6 +279,39 @@ class Model:
                                begin=b, end=en, priority=priority)
         self._engine = e
 
+    def _install_graph(self, e):
+        """Hands the space's adjacency, in buffer order, to engine e."""
+        space = self.get_space()
+        if self._csr is None:
+            src, dst, directed = self._id_edges
+            # buffer slot k holds agent id self._order[k]; the engine maps ids on the GPU
+            e.set_graph_from_ids(self._order.astype(np.int64), src, dst, symmetric=not directed,
+                                 ordered=space.ordered)
+        else:
+            off, idx = self._csr
+            e.set_graph(off, idx, ordered=space.ordered)
+        self._graph_version = space._version
+
+    def _refresh_graph(self):
+        """Topology edited since the engine was built (connect_agents,
+        disconnect_agents, set_csr, set_edges): the new adjacency replaces the
+        device CSR; agent state and tick are kept."""
+        space = self.get_space()
+        if space._version == self._graph_version:
+            return
+        self._id_edges = space._id_edges
+        if self._id_edges is not None:
+            self._csr = None
+        else:
+            from .graphs import permute_csr
+
+            off, idx = space._rows()
+            n = self._order.size
+            if off.size - 1 != n:
+                raise RuntimeError("the space holds %d agents, the model %d" % (off.size - 1, n))
+            self._csr = permute_csr(off, idx, self._pos) if n else (off, idx)
+        self._install_graph(self._engine)
+
     def _refresh_globals(self):
         if not self._globals_dirty:
             return
@@ -306,6 +332,7 @@ class Model:
             self._build_host_arrays()
             self._build_engine()
         self._refresh_globals()
+        self._refresh_graph()
         t0 = time.perf_counter()
         _, tot = self._engine.run(self.tick, int(ticks), stats=self._verbose_timing)
         wall = time.perf_counter() - t0

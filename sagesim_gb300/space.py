@@ -3,8 +3,13 @@
 Same interface and semantics as sagesim/space.py:50-145: add_agent links the
 agent's `locations` property to its container; connect_agents is undirected
 unless directed=True; ordered=True keeps insertion order and drops
-duplicates. set_csr() is an addition for large graphs: it installs a whole
-adjacency at once as CSR arrays (agent ids) without per-edge Python calls.
+duplicates. set_csr() and set_edges() are additions for large graphs: they
+install a whole adjacency at once (CSR arrays or an edge list, in agent ids)
+without per-edge Python calls.
+
+Every change of the adjacency bumps a version counter; a Model that has been
+set up installs the new adjacency at its next simulate() (the reference picks
+up topology edits only when its device buffers are rebuilt).
 """
 import numpy as np
 
@@ -16,6 +21,7 @@ class Space:
         self._agent_factory = None
         self._csr = None
         self._id_edges = None
+        self._version = 0
 
 
 def _network_space_compute_neighbors(agent_locations):
@@ -49,7 +55,11 @@ class NetworkSpace(Space):
             self._locations = [set() for _ in range(total_agents)]
 
     def _materialize(self):
-        """Turns an installed CSR back into per-agent containers (before edits)."""
+        """Turns an installed CSR or edge list back into per-agent containers
+        (before edits)."""
+        if self._id_edges is not None:
+            self._csr = self._edges_to_csr()
+            self._id_edges = None
         if self._csr is None:
             return
         off, idx = self._csr
@@ -73,6 +83,7 @@ class NetworkSpace(Space):
 
     def connect_agents(self, agent_0, agent_1, directed=False):
         self._materialize()
+        self._version += 1
         agent_0 = int(agent_0)
         agent_1 = int(agent_1)
         if self._ordered:
@@ -89,6 +100,7 @@ class NetworkSpace(Space):
 
     def disconnect_agents(self, agent_0, agent_1, directed=False):
         self._materialize()
+        self._version += 1
         agent_0 = int(agent_0)
         agent_1 = int(agent_1)
         if self._ordered:
@@ -111,6 +123,8 @@ class NetworkSpace(Space):
             raise ValueError("CSR has %d rows but the space holds %d agents"
                              % (off.size - 1, len(self._locations)))
         self._csr = (off, idx)
+        self._id_edges = None
+        self._version += 1
 
     def set_edges(self, src_ids, dst_ids, directed=False):
         """Installs the adjacency as an edge list in agent ids (any int64 ids the
@@ -125,9 +139,36 @@ class NetworkSpace(Space):
             raise ValueError("src_ids and dst_ids differ in length")
         self._id_edges = (src, dst, bool(directed))
         self._csr = None
+        self._version += 1
+
+    def _edges_to_csr(self):
+        """CSR (agent ids) of the installed edge list, rows as connect_agents
+        would leave them: each edge added in list order (both directions unless
+        directed), repeats dropped, rows sorted or (ordered) in first-connection
+        order."""
+        src, dst, directed = self._id_edges
+        n = len(self._locations)
+        if src.size and (min(src.min(), dst.min()) < 0 or max(src.max(), dst.max()) >= n):
+            raise ValueError("an edge names an agent id outside 0..%d" % (n - 1))
+        if directed:
+            rows, cols = src, dst
+        else:  # edge k adds src->dst, then dst->src
+            rows = np.stack([src, dst], axis=1).reshape(-1)
+            cols = np.stack([dst, src], axis=1).reshape(-1)
+        key = rows * np.int64(max(n, 1)) + cols
+        _, first = np.unique(key, return_index=True)
+        if self._ordered:
+            first.sort()
+            first = first[np.argsort(rows[first], kind="stable")]
+        rows, cols = rows[first], cols[first]
+        off = np.zeros(n + 1, dtype=np.int32)
+        np.cumsum(np.bincount(rows, minlength=n), out=off[1:])
+        return off, cols.astype(np.int32)
 
     def _rows(self):
         """(offsets, indices) by agent id, from the CSR or the containers."""
+        if self._id_edges is not None:
+            return self._edges_to_csr()
         if self._csr is not None:
             return self._csr
         from .csr import build_csr_from_ragged

@@ -173,3 +173,35 @@ def test_list_property_padded_with_nan():
     assert width == 3 and dt == np.float32
     assert col[0, :2].tolist() == [1.0, 2.0] and np.isnan(col[0, 2]) and col[1].tolist() == [0, 0, 0]
     assert nan != nan
+
+
+@pytest.mark.parametrize("ordered", [False, True])
+@pytest.mark.parametrize("directed", [False, True])
+def test_edge_list_rows_equal_connect_agents(ordered, directed):
+    """set_edges leaves the rows connect_agents would (sagesim/space.py:107-125):
+    repeated and self edges, both directions unless directed, first-connection
+    order for an ordered space; later edits go through the same containers."""
+    rng = np.random.default_rng(5)
+    n = 40
+    src = rng.integers(0, n, 300)
+    dst = rng.integers(0, n, 300)
+    src[:5], dst[:5] = 7, 7  # self edges
+    _, a = make_space(n, ordered=ordered)
+    for s, d in zip(src, dst):
+        a.connect_agents(s, d, directed=directed)
+    _, b = make_space(n, ordered=ordered)
+    v = b._version
+    b.set_edges(src, dst, directed=directed)
+    assert b._version > v
+    off, idx = b._rows()
+    for i in range(n):
+        row = idx[off[i]:off[i + 1]].tolist()
+        assert (row == a.get_location(i)) if ordered else (set(row) == a.get_location(i))
+    b.disconnect_agents(3, 4)
+    a.disconnect_agents(3, 4)
+    assert b._id_edges is None
+    for i in range(n):
+        assert b.get_location(i) == a.get_location(i)
+    with pytest.raises(ValueError):
+        b.set_edges([0], [n])
+        b._rows()

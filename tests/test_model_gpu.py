@@ -334,6 +334,41 @@ def test_global_change_between_simulates():
     assert states(m, 10)[:3] == [2, 2, 1]
 
 
+@pytest.mark.parametrize("first", ["connect", "edges"])
+@pytest.mark.parametrize("strategy", ["count", "pull", "frontier"])
+def test_topology_edits_between_simulates(first, strategy):
+    """Edges added and removed between simulate() calls take effect at the next
+    call, with state and tick kept: the trajectory equals the oracle run on the
+    first adjacency for 10 ticks, then on the edited one from tick 10."""
+    rng = np.random.default_rng(11)
+    n = 3000
+    m, breed = sir_model(SIRStep("B", strategy=strategy), 0.06, 0.1, 17)
+    state0 = np.ones(n, dtype=np.int32)
+    state0[rng.choice(n, 30, replace=False)] = 2
+    for a in range(n):
+        m.create_agent_of_breed(breed, state=int(state0[a]))
+    sp = m.get_space()
+    src, dst = rng.integers(0, n, 6000), rng.integers(0, n, 6000)
+    if first == "edges":
+        sp.set_edges(src, dst)
+    else:
+        for a, b in zip(src, dst):
+            sp.connect_agents(a, b)
+    m.setup()
+    off1, idx1 = sp._rows()
+    m.simulate(10)
+    want, _, _ = oracle.sir_run(2, off1, idx1, state0, 17, 0, 10, 0.06, 0.1)
+    assert np.array_equal(m.get_property_array("state"), want)
+    for a, b in zip(src[:2000], dst[:2000]):
+        sp.disconnect_agents(a, b)
+    for a, b in zip(rng.integers(0, n, 3000), rng.integers(0, n, 3000)):
+        sp.connect_agents(a, b, directed=bool(a & 1))
+    off2, idx2 = sp._rows()
+    m.simulate(10)
+    want, _, _ = oracle.sir_run(2, off2, idx2, want, 17, 10, 10, 0.06, 0.1)
+    assert np.array_equal(m.get_property_array("state"), want)
+
+
 class _PyStepRef:
     """Stands in for a CuPy-JIT rawkernel object: the translator needs only the
     function's name and the module path given to register_step_func."""
