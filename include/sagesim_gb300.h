@@ -26,6 +26,8 @@
  *   sg_add_property               Breed.register_property +
  *                                 property tensor upload        sagesim/breed.py:40-61,
  *                                                               sagesim/model.py:1192-1197
+ *   sg_add_array                  register_breed_local_array +  sagesim/model.py:620-650,
+ *                                 breed-local array build       sagesim/model.py:1215-1270
  *   sg_set_property/get_property  set/get_agent_property_value,
  *                                 get_breed_data                sagesim/model.py:422-490
  *   sg_add_builtin_step           register_step_func (builtin)  sagesim/breed.py:68-99
@@ -185,7 +187,17 @@ int sg_set_globals_f64(sg_engine *e, const double *values, int32_t n);
  * no_double_buffer, sagesim/breed.py:68-99). */
 int sg_add_property(sg_engine *e, const char *name, int32_t dtype, int32_t width,
                     int32_t double_buffered, const void *init, int32_t *prop_id);
-/* Host <-> device copies of agents [first, first+count) of a property. */
+/* Adds a breed-local array (Model.register_breed_local_array,
+ * sagesim/model.py:620-650, storage built at sagesim/model.py:1215-1270):
+ * `rows` rows of `width` values of `dtype`, init holds rows*width values (NULL =
+ * zeros). It is a property whose row count is not the agent count: steps read
+ * and write it through the same property table (ctx.arr_f32 / set_arr_f32),
+ * double-buffered unless double_buffered = 0, and sg_set_property /
+ * sg_get_property / snapshots address its rows. */
+int sg_add_array(sg_engine *e, const char *name, int32_t dtype, int32_t width, int64_t rows,
+                 int32_t double_buffered, const void *init, int32_t *prop_id);
+/* Host <-> device copies of rows [first, first+count) of a property (agents) or
+ * an array. */
 int sg_set_property(sg_engine *e, int32_t prop, const void *host, int64_t first, int64_t count);
 int sg_get_property(sg_engine *e, int32_t prop, void *host, int64_t first, int64_t count);
 /* Device pointer of a property's current (read) buffer, for zero-copy callers. */

@@ -20,7 +20,8 @@
 #define SAGESIM_GB300_STEP_H
 
 /* Per-property device view: two buffers, which one is read at relative tick r
- * is (cur0 + r) & 1 for a double-buffered property, buffer 0 otherwise. */
+ * is (cur0 + r) & 1 for a double-buffered property, buffer 0 otherwise. rows is
+ * the agent count, or the row count of a breed-local array. */
 typedef struct sg_prop_dev {
     void *buf0;
     void *buf1;
@@ -28,6 +29,7 @@ typedef struct sg_prop_dev {
     int dbuf;
     int cur0;
     int dtype;
+    long long rows;
 } sg_prop_dev;
 
 /* Kernel parameter of a compiled step (identical layout on host and device). */
@@ -85,6 +87,23 @@ struct sg_ctx {
     __device__ __forceinline__ void set_f32(int p, int i, float v, int c = 0) const
     {
         ((float *)wr(p))[(long long)i * props[p].width + c] = v;
+    }
+    /* Breed-local arrays (sagesim/model.py:620-650): element (row, c) of the
+     * row-major [rows][width] float32 array p, row from the array's index map
+     * (ctx.i32(p_idx, agent), -1 for agents of other breeds). A row or column
+     * outside the array reads 0 and drops the write. */
+    __device__ __forceinline__ bool in_array(int p, long long row, long long c) const
+    {
+        return (unsigned long long)row < (unsigned long long)props[p].rows &&
+               (unsigned long long)c < (unsigned long long)props[p].width;
+    }
+    __device__ __forceinline__ float arr_f32(int p, long long row, long long c) const
+    {
+        return in_array(p, row, c) ? ((const float *)rd(p))[row * props[p].width + c] : 0.0f;
+    }
+    __device__ __forceinline__ void set_arr_f32(int p, long long row, float v, long long c) const
+    {
+        if (in_array(p, row, c)) ((float *)wr(p))[row * props[p].width + c] = v;
     }
     /* CSR rows: sagesim/utils.py:36-57 (get_num_neighbors / get_neighbor). */
     __device__ __forceinline__ int degree(int i) const { return off[i + 1] - off[i]; }

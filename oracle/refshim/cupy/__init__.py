@@ -8,12 +8,27 @@ import numpy as _np
 from . import cuda  # noqa: F401
 
 
+def _plain_index(idx):
+    """Integer 0-d arrays (what element reads return here) as Python ints, so
+    that a[i][j] = v with i read from another array writes through a view, as
+    the pointer arithmetic of a CuPy-JIT kernel does; numpy would treat a 0-d
+    array index as advanced indexing and assign into a copy."""
+    if isinstance(idx, _np.ndarray) and idx.ndim == 0 and idx.dtype.kind in "iu":
+        return int(idx)
+    if isinstance(idx, tuple):
+        return tuple(_plain_index(i) for i in idx)
+    return idx
+
+
 class ndarray(_np.ndarray):
     def get(self):
         return _np.asarray(self).copy()
 
+    def __setitem__(self, idx, value):
+        _np.ndarray.__setitem__(self, _plain_index(idx), value)
+
     def __getitem__(self, idx):
-        out = _np.ndarray.__getitem__(self, idx)
+        out = _np.ndarray.__getitem__(self, _plain_index(idx))
         if isinstance(out, _np.ndarray):
             return out
         # CuPy indexing yields 0-d device arrays that still carry .get()

@@ -30,6 +30,7 @@ struct SgProp {
     std::string name;
     int32_t dtype = SG_I32;
     int32_t width = 1;
+    int64_t rows = 0; // agents, or the rows of a breed-local array
     bool dbuf = true;
     int cur = 0; // read buffer
     SgDev buf[2];
@@ -348,24 +349,26 @@ int sg_set_globals_f64(sg_engine *e, const double *values, int32_t n)
     return SG_OK;
 }
 
-int sg_add_property(sg_engine *e, const char *name, int32_t dtype, int32_t width,
+static int add_prop(sg_engine *e, const char *name, int32_t dtype, int32_t width, int64_t rows,
                     int32_t double_buffered, const void *init, int32_t *prop_id)
 {
     if (!e || !name || !prop_id) return SG_ERR_INVALID;
     if (e->n < 0) return e->fail(SG_ERR_INVALID, "set the graph before adding properties");
     if (dtype != SG_I32 && dtype != SG_F32) return e->fail(SG_ERR_INVALID, "dtype must be SG_I32 or SG_F32");
     if (width < 1 || width > 4096) return e->fail(SG_ERR_INVALID, "width out of range");
+    if (rows < 0 || rows > ((int64_t)1 << 31) - 1) return e->fail(SG_ERR_INVALID, "row count out of range");
     cudaSetDevice(e->device);
     auto p = std::make_unique<SgProp>();
     p->name = name;
     p->dtype = dtype;
     p->width = width;
+    p->rows = rows;
     p->dbuf = double_buffered != 0;
-    const size_t bytes = (size_t)std::max<int64_t>(e->n, 1) * p->row_bytes();
+    const size_t bytes = (size_t)std::max<int64_t>(rows, 1) * p->row_bytes();
     SG_CK(p->buf[0].reserve(bytes));
     if (p->dbuf) SG_CK(p->buf[1].reserve(bytes));
-    if (init && e->n > 0)
-        SG_CK(cudaMemcpyAsync(p->buf[0].p, init, (size_t)e->n * p->row_bytes(), cudaMemcpyHostToDevice,
+    if (init && rows > 0)
+        SG_CK(cudaMemcpyAsync(p->buf[0].p, init, (size_t)rows * p->row_bytes(), cudaMemcpyHostToDevice,
                               e->stream));
     else
         SG_CK(cudaMemsetAsync(p->buf[0].p, 0, bytes, e->stream));
@@ -377,11 +380,25 @@ int sg_add_property(sg_engine *e, const char *name, int32_t dtype, int32_t width
     return SG_OK;
 }
 
+int sg_add_property(sg_engine *e, const char *name, int32_t dtype, int32_t width,
+                    int32_t double_buffered, const void *init, int32_t *prop_id)
+{
+    if (!e) return SG_ERR_INVALID;
+    return add_prop(e, name, dtype, width, e->n, double_buffered, init, prop_id);
+}
+
+int sg_add_array(sg_engine *e, const char *name, int32_t dtype, int32_t width, int64_t rows,
+                 int32_t double_buffered, const void *init, int32_t *prop_id)
+{
+    if (!e) return SG_ERR_INVALID;
+    return add_prop(e, name, dtype, width, rows, double_buffered, init, prop_id);
+}
+
 static int check_range(sg_engine *e, int32_t prop, int64_t first, int64_t count)
 {
     if (prop < 0 || prop >= (int32_t)e->props.size()) return e->fail(SG_ERR_NOT_FOUND, "unknown property");
-    if (first < 0 || count < 0 || first + count > e->n)
-        return e->fail(SG_ERR_INVALID, "agent range out of bounds");
+    if (first < 0 || count < 0 || first + count > e->props[prop]->rows)
+        return e->fail(SG_ERR_INVALID, "row range out of bounds");
     return SG_OK;
 }
 
@@ -433,6 +450,7 @@ int sg_add_builtin_step(sg_engine *e, const sg_builtin_params *bp, int32_t *step
     const SgProp &sp = *e->props[bp->state_prop];
     if (!sp.dbuf) return e->fail(SG_ERR_INVALID, "builtin steps need a double-buffered state property");
     if (sp.width != 1) return e->fail(SG_ERR_INVALID, "state property must have width 1");
+    if (sp.rows != e->n) return e->fail(SG_ERR_INVALID, "state property must be an agent property, not an array");
     if (bp->begin < 0 || bp->end > e->n || bp->begin > bp->end)
         return e->fail(SG_ERR_INVALID, "step agent range out of bounds");
     if (bp->builtin == SG_BUILTIN_SIR_A || bp->builtin == SG_BUILTIN_SIR_B) {
@@ -441,7 +459,8 @@ int sg_add_builtin_step(sg_engine *e, const sg_builtin_params *bp, int32_t *step
             return e->fail(SG_ERR_INVALID, "unknown SIR strategy");
     } else if (bp->builtin == SG_BUILTIN_OPINION) {
         if (sp.dtype != SG_F32) return e->fail(SG_ERR_INVALID, "opinion must be float32");
-        if (bp->aux_prop < 0 || bp->aux_prop >= nprops || e->props[bp->aux_prop]->dtype != SG_F32)
+        if (bp->aux_prop < 0 || bp->aux_prop >= nprops || e->props[bp->aux_prop]->dtype != SG_F32 ||
+            e->props[bp->aux_prop]->rows != e->n)
             return e->fail(SG_ERR_INVALID, "opinion needs a float32 weights property (aux_prop)");
     } else {
         return e->fail(SG_ERR_INVALID, "unknown builtin");
@@ -737,7 +756,7 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
             const int rd = (pp.cur + r) & 1;
             SG_PROF_LAUNCH("copy_through",
                            sg_launch_copy_words(pp.buf[rd].as<uint32_t>(), pp.buf[rd ^ 1].as<uint32_t>(),
-                                                e->n * pp.width, e->stream));
+                                                pp.rows * pp.width, e->stream));
         }
         for (SgStep *s : pl.order) {
             const bool inplace = pl.count_inplace && s == pl.count_step;
@@ -830,9 +849,9 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
             const bool swaps = p.dbuf && std::find(pl.swap_props.begin(), pl.swap_props.end(), (int32_t)k) !=
                                              pl.swap_props.end();
             if (swaps)
-                tab.push_back(sg_prop_dev{p.buf[0].p, p.buf[1].p, p.width, 1, p.cur, p.dtype});
+                tab.push_back(sg_prop_dev{p.buf[0].p, p.buf[1].p, p.width, 1, p.cur, p.dtype, (long long)p.rows});
             else
-                tab.push_back(sg_prop_dev{p.buf[p.cur].p, p.buf[p.cur].p, p.width, 0, 0, p.dtype});
+                tab.push_back(sg_prop_dev{p.buf[p.cur].p, p.buf[p.cur].p, p.width, 0, 0, p.dtype, (long long)p.rows});
         }
         SG_CK(e->prop_table.reserve(std::max<size_t>(tab.size(), 1) * sizeof(sg_prop_dev)));
         if (!tab.empty())
@@ -1050,7 +1069,7 @@ int sg_snapshot(sg_engine *e)
     if (!e) return SG_ERR_INVALID;
     cudaSetDevice(e->device);
     for (auto &p : e->props) {
-        const size_t bytes = (size_t)std::max<int64_t>(e->n, 1) * p->row_bytes();
+        const size_t bytes = (size_t)std::max<int64_t>(p->rows, 1) * p->row_bytes();
         SG_CK(p->snap.reserve(bytes));
         SG_CK(cudaMemcpyAsync(p->snap.p, p->buf[p->cur].p, bytes, cudaMemcpyDeviceToDevice, e->stream));
     }
@@ -1064,7 +1083,7 @@ int sg_restore(sg_engine *e)
     cudaSetDevice(e->device);
     for (auto &p : e->props) {
         if (!p->snap.p) return e->fail(SG_ERR_INVALID, "no snapshot");
-        const size_t bytes = (size_t)std::max<int64_t>(e->n, 1) * p->row_bytes();
+        const size_t bytes = (size_t)std::max<int64_t>(p->rows, 1) * p->row_bytes();
         SG_CK(cudaMemcpyAsync(p->buf[p->cur].p, p->snap.p, bytes, cudaMemcpyDeviceToDevice, e->stream));
     }
     return SG_OK;

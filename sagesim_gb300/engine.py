@@ -110,11 +110,27 @@ class Engine:
         pid = ctypes.c_int32()
         self._ck(self._lib.sg_add_property(self._h, name.encode(), dt, int(width),
                                            1 if double_buffered else 0, _ptr(a), ctypes.byref(pid)))
-        self._props[pid.value] = (npdt, int(width))
+        self._props[pid.value] = (npdt, int(width), self.n)
+        return pid.value
+
+    def add_array(self, name, dtype, width, rows, init=None, double_buffered=True):
+        """A breed-local array: `rows` rows of `width` values (zeros unless init),
+        addressed by row in steps and in get/set_property."""
+        dt = N.SG_I32 if np.dtype(dtype) == np.int32 else N.SG_F32
+        npdt = np.int32 if dt == N.SG_I32 else np.float32
+        a = None
+        if init is not None:
+            a = np.ascontiguousarray(init, dtype=npdt).reshape(-1)
+            if a.size != rows * width:
+                raise ValueError("init must hold rows*width values")
+        pid = ctypes.c_int32()
+        self._ck(self._lib.sg_add_array(self._h, name.encode(), dt, int(width), int(rows),
+                                        1 if double_buffered else 0, _ptr(a), ctypes.byref(pid)))
+        self._props[pid.value] = (npdt, int(width), int(rows))
         return pid.value
 
     def set_property(self, prop, values, first=0):
-        npdt, width = self._props[prop]
+        npdt, width, _ = self._props[prop]
         a = np.ascontiguousarray(values, dtype=npdt).reshape(-1)
         if a.size % width:
             raise ValueError("values must hold whole rows")
@@ -125,9 +141,9 @@ class Engine:
         self._ck(self._lib.sg_set_property(self._h, prop, ctypes.c_void_p(host_ptr), int(first), int(count)))
 
     def get_property(self, prop, first=0, count=None):
-        npdt, width = self._props[prop]
+        npdt, width, rows = self._props[prop]
         if count is None:
-            count = self.n - first
+            count = rows - first
         out = np.empty(count * width, dtype=npdt)
         self._ck(self._lib.sg_get_property(self._h, prop, _ptr(out), int(first), int(count)))
         return out.reshape(count, width) if width > 1 else out

@@ -123,7 +123,32 @@ class Model:
         self._partition_file = partition_file
 
     def register_breed_local_array(self, name, breed, shape_per_agent, neighbor_visible=False):
-        raise NotImplementedError("breed-local arrays are not supported by this engine yet")
+        """sagesim/model.py:620-645: a float32 array with one row of
+        shape_per_agent per agent of `breed`, zeros at setup. Every step function
+        receives it after the properties as two parameters, the array and its
+        index map (row of agent i = idx[i], -1 for agents of other breeds). A
+        written array is double-buffered unless a step's no_double_buffer names
+        it. neighbor_visible adds ghost rows across ranks in the reference; on one
+        GPU every row is local."""
+        if self._is_setup:
+            raise RuntimeError("register breed-local arrays before setup()")
+        shape = tuple(int(d) for d in np.atleast_1d(shape_per_agent))
+        if not shape or min(shape) < 1:
+            raise ValueError("shape_per_agent must hold positive sizes")
+        if any(b["name"] == name for b in self._breed_local_arrays):
+            raise ValueError("breed-local array %r is already registered" % name)
+        self._breed_local_arrays.append({"name": name, "breed": breed, "shape_per_agent": shape,
+                                         "neighbor_visible": bool(neighbor_visible)})
+        return len(self._breed_local_arrays) - 1
+
+    def get_breed_local_array(self, name):
+        """sagesim/model.py:647-650: the array's current contents, shape
+        (rows, *shape_per_agent), rows = the breed's agent count (at least 1)."""
+        bla = next(b for b in self._breed_local_arrays if b["name"] == name)
+        if self._engine is None:
+            raise RuntimeError("breed-local arrays live on the device: call setup() first")
+        a = self._engine.get_property(self._pid["sgbla_" + name])
+        return a.reshape((-1,) + bla["shape_per_agent"])
 
     # ---- setup -------------------------------------------------------------------------
     def setup(self, use_gpu=True, skip_priority_barriers=False):
@@ -243,12 +268,26 @@ class Model:
         # Python-dialect steps: globals and properties mapped by position
         gnames = [k for k, _ in sorted(self._global_names.items(), key=lambda kv: kv[1])]
         pdt = {k: ("i" if v[0] == np.int32 else "f") for k, v in self._props.items()}
-        self._steps = [(pr, bi, (fn.translate(gnames, list(self._props), pdt) if isinstance(fn, PythonStep) else fn),
-                        path) for pr, bi, fn, path in self._steps]
+        arrays = [(b["name"], b["shape_per_agent"]) for b in self._breed_local_arrays]
+        self._steps = [(pr, bi, (fn.translate(gnames, list(self._props), pdt, arrays) if isinstance(fn, PythonStep)
+                                 else fn), path) for pr, bi, fn, path in self._steps]
         self._pid = {}
         for name, (dt, width, arr) in self._props.items():
             self._pid[name] = e.add_property(name, dt, width, init=arr,
                                              double_buffered=name not in self._no_double_buffer)
+        # breed-local arrays (sagesim/model.py:1215-1270): rows in breed-range
+        # order, index map from buffer index to row
+        n = self._order.size
+        for bla in self._breed_local_arrays:
+            b, en = self._breed_ranges.get(bla["breed"]._breedidx, (0, 0))
+            width = int(np.prod(bla["shape_per_agent"]))
+            key = "sgbla_" + bla["name"]
+            self._pid[key] = e.add_array(key, np.float32, width, max(en - b, 1),
+                                         double_buffered=bla["name"] not in self._no_double_buffer)
+            idx_map = np.full(n, -1, dtype=np.int32)
+            idx_map[b:en] = np.arange(en - b, dtype=np.int32)
+            self._pid[key + "_idx"] = e.add_property(key + "_idx", np.int32, 1, init=idx_map,
+                                                     double_buffered=False)
         writers = {}
         for _, bidx, fn, _ in self._steps:
             for w in fn.writes:

@@ -62,7 +62,7 @@ class OpinionStep:
 class CudaStep:
     """A CUDA C++ step: `source` defines `__device__ void <entry>(const sg_ctx&, int i)`."""
 
-    _SET = re.compile(r"set_(?:i32|f32)\s*\(\s*PROP_(\w+)")
+    _SET = re.compile(r"set_(?:i32|f32|arr_f32)\s*\(\s*PROP_(\w+)")
 
     def __init__(self, source, entry, writes=None):
         self.source = source
@@ -88,10 +88,11 @@ class PythonStep:
         self.source, self.name = find_step_source(step_func, module_fpath)
         self._writes = None
 
-    def translate(self, globals_, props, prop_dtypes):
+    def translate(self, globals_, props, prop_dtypes, arrays=()):
         from .translate import translate_step
 
-        src, entry, writes = translate_step(self.source, self.name, globals_, props, prop_dtypes)
+        src, entry, writes = translate_step(self.source, self.name, globals_, props, prop_dtypes,
+                                            arrays=arrays)
         self._writes = tuple(writes)
         return CudaStep(src, entry, writes=list(writes))
 

@@ -101,7 +101,7 @@ def _promote(a, b):
 
 
 class _Translator:
-    def __init__(self, fn, globals_, props, prop_dtypes, entry):
+    def __init__(self, fn, globals_, props, prop_dtypes, entry, arrays=()):
         self.fn = fn
         self.entry = entry
         args = [a.arg for a in fn.args.args]
@@ -125,6 +125,18 @@ class _Translator:
                 self.locations = a
             else:
                 self.props[a] = p
+        # breed-local arrays: (array, index map) parameter pairs after the
+        # properties, in registration order (sagesim/model.py:1994-2008)
+        self.arrays = {}  # parameter -> (array name, shape per agent)
+        self.array_idx = {}  # parameter -> array name
+        tail = rest[1 + len(pnames):]
+        arrays = list(arrays)
+        if len(tail) != 2 * len(arrays):
+            raise StepTranslationError("%s: expected %d breed-local array parameters after the properties, got %d"
+                                       % (fn.name, 2 * len(arrays), len(tail)))
+        for k, (aname, shape) in enumerate(arrays):
+            self.arrays[tail[2 * k]] = (aname, tuple(int(d) for d in shape))
+            self.array_idx[tail[2 * k + 1]] = aname
         self.prop_dtypes = prop_dtypes
         self.locals = {}  # name -> type
         self.row_of = {}  # row local -> agent expression
@@ -233,8 +245,36 @@ class _Translator:
             return "ctx.%s(PROP_%s, (int)(%s))" % (fn, pname, agent), ("i" if dt == "i" else "f")
         return "ctx.%s(PROP_%s, (int)(%s), (int)(%s))" % (fn, pname, agent, comp), ("i" if dt == "i" else "f")
 
+    def array_element(self, n):
+        """(array name, row C++, column C++) when n is a full element of a
+        breed-local array (a[r][j], a[r, j], a[r][j][k], a[r, j, k]), else None."""
+        subs = []
+        b = n
+        while isinstance(b, ast.Subscript):
+            sl = b.slice
+            subs[:0] = list(sl.elts) if isinstance(sl, ast.Tuple) else [sl]
+            b = b.value
+        if not (isinstance(b, ast.Name) and b.id in self.arrays):
+            return None
+        aname, shape = self.arrays[b.id]
+        if len(subs) != 1 + len(shape):
+            self.err(n, "breed-local array %r needs %d indices" % (aname, 1 + len(shape)))
+        row, _ = self.expr(subs[0])
+        col = "0LL"
+        for d, sub in zip(shape, subs[1:]):
+            c, _ = self.expr(sub)
+            col = "(%s) * %dLL + (long long)(%s)" % (col, d, c)
+        return aname, row, col
+
     def subscript(self, n):
+        el = self.array_element(n)
+        if el is not None:
+            aname, row, col = el
+            return "ctx.arr_f32(PROP_sgbla_%s, (long long)(%s), %s)" % (aname, row, col), "f"
         base, idx = n.value, n.slice
+        if isinstance(base, ast.Name) and base.id in self.array_idx:
+            a, _ = self.expr(idx)
+            return "(long long)ctx.i32(PROP_sgbla_%s_idx, (int)(%s))" % (self.array_idx[base.id], a), "i"
         # p[a][c]
         if isinstance(base, ast.Subscript) and isinstance(base.value, ast.Name) and base.value.id in self.props:
             a, _ = self.expr(base.slice)
@@ -334,7 +374,8 @@ class _Translator:
     # ---- statements ------------------------------------------------------------------
     def declare(self, name, t, node):
         t = "i" if t == "wi" else ("d" if t == "wf" else t)
-        if name in (self.tick, self.agent) or name in self.globals or name in self.props:
+        if (name in (self.tick, self.agent) or name in self.globals or name in self.props
+                or name in self.arrays or name in self.array_idx):
             self.err(node, "cannot assign to parameter %r" % name)
         old = self.locals.get(name)
         if old is None:
@@ -441,6 +482,13 @@ class _Translator:
             t = self.locals[tgt.id]
             return self.emit("u_%s = (%s)(%s);" % (tgt.id, _CT[t], v), d)
         if isinstance(tgt, ast.Subscript):
+            el = self.array_element(tgt)
+            if el is not None:
+                aname, row, col = el
+                v, _ = self.expr(value)
+                self.writes.add("sgbla_" + aname)
+                return self.emit("ctx.set_arr_f32(PROP_sgbla_%s, (long long)(%s), (float)(%s), %s);"
+                                 % (aname, row, v, col), d)
             base, idx = tgt.value, tgt.slice
             comp = None
             if isinstance(base, ast.Subscript) and isinstance(base.value, ast.Name) and base.value.id in self.props:
@@ -481,13 +529,17 @@ def _load(t):
     return n
 
 
-def translate_step(source, name, globals_, props, prop_dtypes, entry=None):
+def translate_step(source, name, globals_, props, prop_dtypes, entry=None, arrays=()):
     """CUDA C++ for step `name` defined in `source`.
 
     globals_: the model's global property names in registration order.
     props: the model's agent property names in property order (without the
     breed and the neighbour rows). prop_dtypes: name -> "i" (int32) or "f"
-    (float32). Returns (C++ source, entry name, properties written)."""
+    (float32). arrays: the model's breed-local arrays in registration order as
+    (name, shape per agent); each is read and written as the float32 engine
+    array PROP_sgbla_<name> (row-major, one row per agent of its breed) with the
+    int32 index map PROP_sgbla_<name>_idx. Returns (C++ source, entry name,
+    properties and arrays written, the arrays as sgbla_<name>)."""
     tree = ast.parse(source)
     fn = None
     for node in ast.walk(tree):
@@ -497,5 +549,5 @@ def translate_step(source, name, globals_, props, prop_dtypes, entry=None):
     if fn is None:
         raise StepTranslationError("no function %r in the step's source" % name)
     entry = entry or ("sg_py_" + name)
-    tr = _Translator(fn, list(globals_), list(props), dict(prop_dtypes), entry)
+    tr = _Translator(fn, list(globals_), list(props), dict(prop_dtypes), entry, arrays)
     return tr.run(), entry, sorted(tr.writes)

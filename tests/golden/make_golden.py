@@ -21,6 +21,10 @@ Outputs (committed; the tests read only these files):
                        (SIR-B); state after every tick
   ba_breeds.npz        3,000-agent BA graph, two interleaved breeds, explicit
                        logical ids for some agents, SIR-B, 30 ticks
+  bla_two_breeds.npz   1,500-agent BA graph, host and site breeds with
+                       breed-local arrays (one double-buffered, one written in
+                       place at a later priority), both arrays after ticks
+                       1, 2, 3, 5, 10, 25
   opinion_ws.npz       2,000-agent WS graph (k=10, p=0.1, seed 2), ordered
                        neighbours, float32 opinion + float32[8] weights, 50 ticks
 """
@@ -256,6 +260,56 @@ def opinion_ws():
                         weights=w, ticks=keep, history=hist[keep - 1])
 
 
+def bla_two_breeds():
+    from ref_steps import host_step, site_step
+    from sagesim.breed import Breed
+    from sagesim.model import Model
+    from sagesim.space import NetworkSpace
+
+    from sagesim_gb300 import graphs
+
+    off, idx = graphs.barabasi_albert(1500, 3, 8)
+    n = off.size - 1
+    rng = np.random.default_rng(8)
+    breeds = (rng.random(n) < 0.4).astype(np.int32)  # 1 = site
+    st = np.ones(n, dtype=np.int32)
+    hosts = np.flatnonzero(breeds == 0)
+    st[rng.choice(hosts, 20, replace=False)] = 2
+    model = Model(NetworkSpace(), step_function_file_path="step_func_code_gold_bla.py")
+    host, site = Breed("Host"), Breed("Site")
+    for br in (host, site):
+        br.register_property("state", 1)
+    path = os.path.join(HERE, "ref_steps.py")
+    host.register_step_func(host_step, path, priority=0)
+    site.register_step_func(site_step, path, priority=1, no_double_buffer=["load"])
+    model.register_breed(host)
+    model.register_breed(site)
+    model.register_global_property("p_infection", 0.04)
+    model.register_global_property("p_recovery", 0.1)
+    model.register_breed_local_array("health", host, (4,))
+    model.register_breed_local_array("load", site, (2, 2))
+    model.set_seed(8)
+    for i in range(n):
+        model.create_agent_of_breed(site if breeds[i] else host, state=int(st[i]))
+    sp = model.get_space()
+    for i in range(n):
+        for k in range(off[i], off[i + 1]):
+            sp.connect_agents(i, int(idx[k]), directed=True)
+    model._max_blocks_per_sm = 1
+    model.setup(use_gpu=True)
+    keep = [1, 2, 3, 5, 10, 25]
+    health, load = [], []
+    for t in range(1, keep[-1] + 1):
+        model.simulate(1, sync_workers_every_n_ticks=1)
+        if t in keep:
+            health.append(np.asarray(model.get_breed_local_array("health"), dtype=np.float32))
+            load.append(np.asarray(model.get_breed_local_array("load"), dtype=np.float32))
+    clear_generated()
+    np.savez_compressed(os.path.join(HERE, "bla_two_breeds.npz"), offsets=off, indices=idx, breeds=breeds,
+                        state0=st.astype(np.int8), ticks=np.array(keep), health=np.stack(health),
+                        load=np.stack(load))
+
+
 def main():
     reference = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SAGESIM_REFERENCE", "")
     if not reference or not os.path.isdir(os.path.join(reference, "sagesim")):
@@ -263,9 +317,9 @@ def main():
     setup_paths(reference)
     work = tempfile.mkdtemp(prefix="sg_golden_")
     os.chdir(work)  # the reference writes its generated step module into the CWD
-    which = sys.argv[2:] or ["philox", "chain", "hier", "db", "er", "breeds", "opinion"]
+    which = sys.argv[2:] or ["philox", "chain", "hier", "db", "er", "breeds", "bla", "opinion"]
     jobs = {"philox": philox_vectors, "chain": chains, "hier": hierarchy, "db": db_priority,
-            "er": er_c1, "breeds": ba_breeds, "opinion": opinion_ws}
+            "er": er_c1, "breeds": ba_breeds, "bla": bla_two_breeds, "opinion": opinion_ws}
     for w in which:
         print("generating", w, flush=True)
         jobs[w]()

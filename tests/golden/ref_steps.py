@@ -9,6 +9,15 @@ sir_per_neighbour_step: per-infected-neighbour SIR. An infected agent recovers
   when philox(salt 1) < p_recovery. A susceptible agent scans its neighbours in
   CSR order; the j-th infected neighbour found (j = 0, 1, ...) draws
   philox(salt 2 + j) and the first draw below p_infection infects it.
+host_step / site_step: two breeds with breed-local arrays and no property
+  writes. Hosts keep health[row] = (status 0 S / 1 I / 2 R, decayed
+  infected-neighbour count, ticks infected, sum of the neighbouring hosts'
+  decayed counts) in a double-buffered float32[4] array (status read from the
+  int property state - 1 at tick 0); a susceptible host is infected with
+  probability p_infection * (decayed count + 0.1 * neighbouring sites' load).
+  Sites (priority 1) write load[row][tick % 2] = (neighbouring hosts' ticks
+  infected, infected neighbouring hosts at tick start) in place
+  (no_double_buffer) and add 0.5 to the other slot's count.
 opinion_step: weighted mean of the first min(deg, 8) ordered neighbours'
   opinions (float32 arithmetic in row order, normalised by the sum of |w|),
   plus noise_sigma * rand_normal(salt 1) in float64, clamped to [0, 1].
@@ -73,3 +82,75 @@ def opinion_step(
     if y > 1.0:
         y = 1.0
     opinion[agent_index] = y
+
+
+
+@jit.rawkernel(device="cuda")
+def host_step(
+    tick, agent_index, p_infection, p_recovery,
+    agent_ids, breeds, locations, state_tensor,
+    health, health_idx, load, load_idx,
+):
+    row = health_idx[agent_index]
+    neighbor_indices = locations[agent_index]
+    k = 0
+    e_n = cp.float32(0.0)
+    site_load = cp.float32(0.0)
+    i = 0
+    while i < len(neighbor_indices):
+        nb = int(neighbor_indices[i])
+        r2 = health_idx[nb]
+        if r2 >= 0:
+            if tick == 0:
+                s2 = int(state_tensor[nb]) - 1
+            else:
+                s2 = int(health[r2][0])
+            if s2 == 1:
+                k += 1
+            e_n = cp.float32(e_n + health[r2][1])
+        r3 = load_idx[nb]
+        if r3 >= 0:
+            site_load = cp.float32(site_load + load[r3][1][0])
+        i += 1
+    if tick == 0:
+        s = int(state_tensor[agent_index]) - 1
+    else:
+        s = int(health[row][0])
+    ex = cp.float32(health[row][1])
+    health[row][1] = cp.float32(cp.float32(ex * cp.float32(0.5)) + cp.float32(k))
+    health[row, 3] = e_n
+    new = s
+    if s == 1:
+        health[row][2] += cp.float32(1.0)
+        if rand_uniform_philox(tick, agent_index, 1) < p_recovery:
+            new = 2
+    elif s == 0:
+        p = p_infection * (float(ex) + 0.1 * float(site_load))
+        if rand_uniform_philox(tick, agent_index, 2) < p:
+            new = 1
+    health[row][0] = cp.float32(new)
+
+
+@jit.rawkernel(device="cuda")
+def site_step(
+    tick, agent_index, p_infection, p_recovery,
+    agent_ids, breeds, locations, state_tensor,
+    health, health_idx, load, load_idx,
+):
+    row = load_idx[agent_index]
+    neighbor_indices = locations[agent_index]
+    tot = cp.float32(0.0)
+    k = 0
+    i = 0
+    while i < len(neighbor_indices):
+        nb = int(neighbor_indices[i])
+        r2 = health_idx[nb]
+        if r2 >= 0:
+            tot = cp.float32(tot + health[r2][2])
+            if int(health[r2][0]) == 1:
+                k = k + 1
+        i += 1
+    slot = tick % 2
+    load[row][slot][0] = tot
+    load[row][slot][1] = cp.float32(k)
+    load[row][1 - slot][1] += cp.float32(0.5)

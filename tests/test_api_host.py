@@ -205,3 +205,22 @@ def test_edge_list_rows_equal_connect_agents(ordered, directed):
     with pytest.raises(ValueError):
         b.set_edges([0], [n])
         b._rows()
+
+
+def test_breed_local_array_registration():
+    """sagesim/model.py:620-645: index in registration order; our checks refuse
+    a repeated name, empty shapes and registration after setup."""
+    m, _ = make_space(3)
+    b = list(m._agent_factory.breeds)[0]
+    assert m.register_breed_local_array("h", b, (4,)) == 0
+    assert m.register_breed_local_array("g", b, 5) == 1
+    assert m._breed_local_arrays[1]["shape_per_agent"] == (5,)
+    with pytest.raises(ValueError):
+        m.register_breed_local_array("h", b, (2,))
+    with pytest.raises(ValueError):
+        m.register_breed_local_array("z", b, (0,))
+    with pytest.raises(RuntimeError):
+        m.get_breed_local_array("h")
+    m._is_setup = True
+    with pytest.raises(RuntimeError):
+        m.register_breed_local_array("late", b, (1,))

@@ -427,3 +427,43 @@ def test_python_dialect_opinion_step_matches_reference():
         rel = np.abs(got - want) / np.maximum(np.abs(want), 1e-30)
         ok = (rel <= 1e-6) | (np.abs(got - want) <= 1e-12)
         assert ok.all(), "tick %d: max rel %g" % (t, rel[~ok].max())
+
+
+def test_breed_local_arrays_match_reference():
+    """Two breeds with breed-local arrays (sagesim/model.py:620-650,
+    1215-1270): the hosts' double-buffered float32[4] array and the sites'
+    in-place float32[2][2] array written at priority 1, both translated from the
+    reference dialect, equal the reference pipeline's arrays bit for bit."""
+    d = gold("bla_two_breeds.npz")
+    off, idx, breeds, st = d["offsets"], d["indices"], d["breeds"], d["state0"]
+    n = off.size - 1
+    m = Model(NetworkSpace())
+    host, site = Breed("Host"), Breed("Site")
+    for br in (host, site):
+        br.register_property("state", 1)
+    host.register_step_func(_PyStepRef("host_step"), REF_STEPS, priority=0)
+    site.register_step_func(_PyStepRef("site_step"), REF_STEPS, priority=1, no_double_buffer=["load"])
+    m.register_breed(host)
+    m.register_breed(site)
+    m.register_global_property("p_infection", 0.04)
+    m.register_global_property("p_recovery", 0.1)
+    assert m.register_breed_local_array("health", host, (4,)) == 0
+    assert m.register_breed_local_array("load", site, (2, 2)) == 1
+    m.set_seed(8)
+    for i in range(n):
+        m.create_agent_of_breed(site if breeds[i] else host, state=int(st[i]))
+    sp = m.get_space()
+    for i in range(n):
+        for k in range(off[i], off[i + 1]):
+            sp.connect_agents(i, int(idx[k]), directed=True)
+    m.setup()
+    assert not m.get_breed_local_array("health").any()
+    for j, t in enumerate(d["ticks"]):
+        m.simulate(int(t) - m.tick)
+        h, ld = m.get_breed_local_array("health"), m.get_breed_local_array("load")
+        assert h.shape == d["health"][j].shape and ld.shape == d["load"][j].shape
+        assert np.array_equal(h, d["health"][j]), "health, tick %d" % t
+        assert np.array_equal(ld, d["load"][j]), "load, tick %d" % t
+    m.reset()
+    m.simulate(1)
+    assert np.array_equal(m.get_breed_local_array("health"), d["health"][0])  # rebuilt from zeros

@@ -91,3 +91,31 @@ def test_missing_function_and_short_signature():
         _tr("def other(tick, agent_index):\n    pass\n")
     with pytest.raises(StepTranslationError, match="expected"):
         _tr("def step(tick, agent_index):\n    pass\n", globals_=("a", "b"))
+
+
+def test_breed_local_arrays():
+    """Breed-local arrays come as (array, index map) parameter pairs after the
+    properties (sagesim/model.py:1994-2008); elements are flattened row-major
+    into the engine array, writes are reported as sgbla_<name>."""
+    src = open(os.path.join(GOLD, "ref_steps.py")).read()
+    arrays = [("health", (4,)), ("load", (2, 2))]
+    code, _, writes = translate_step(src, "host_step", ["p_infection", "p_recovery"], ["state"], {"state": "i"},
+                                     arrays=arrays)
+    assert writes == ["sgbla_health"]
+    assert "(long long)ctx.i32(PROP_sgbla_health_idx, (int)(sg_agent))" in code
+    assert "ctx.arr_f32(PROP_sgbla_load, (long long)(u_r3), ((0LL) * 2LL + (long long)(1LL)) * 2LL + (long long)(0LL))" in code
+    assert "ctx.set_arr_f32(PROP_sgbla_health, (long long)(u_row), (float)(u_e_n), (0LL) * 4LL + (long long)(3LL));" in code
+    _, _, writes = translate_step(src, "site_step", ["p_infection", "p_recovery"], ["state"], {"state": "i"},
+                                  arrays=arrays)
+    assert writes == ["sgbla_load"]
+    bad = '''
+def step(tick, agent_index, p, agent_ids, breeds, locations, state, h, h_idx):
+    h[h_idx[agent_index]] = 1.0
+'''
+    with pytest.raises(StepTranslationError, match="needs 2 indices"):
+        translate_step(bad, "step", ["p"], ["state"], {"state": "i"}, arrays=[("h", (3,))])
+    with pytest.raises(StepTranslationError, match="breed-local array parameters"):
+        translate_step(bad, "step", ["p"], ["state"], {"state": "i"})
+    bad = bad.replace("h[h_idx[agent_index]] = 1.0", "h_idx[agent_index] = 1")
+    with pytest.raises(StepTranslationError):
+        translate_step(bad, "step", ["p"], ["state"], {"state": "i"}, arrays=[("h", (3,))])
