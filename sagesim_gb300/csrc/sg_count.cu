@@ -86,6 +86,60 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_init_kernel(SgTickAr
     }
 }
 
+// Count init by scattering from the infected agents, for a step over every
+// agent of a graph with one segment (the usual single-model case). The clear
+// pass zeroes the counts and the activity words and writes the class bytes; the
+// scatter pass walks the transpose row of each infected agent (one warp per
+// infected agent, coalesced) adding 1 to every neighbour's count and setting
+// the activity bit of susceptible neighbours. The counts equal the per-row
+// scan of sir_count_init_kernel; the work is the infected agents' degree sum
+// instead of every row, which at the start of an outbreak is a small fraction.
+__global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_init_clear_kernel(SgTickArgs a)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+        const SgTile tile = a.tiles[t];
+        const SgSeg &sg = a.segs[tile.seg];
+        const int32_t *__restrict__ sin = (const int32_t *)((sg.par0 & 1) ? a.buf1 : a.buf0);
+        for (int32_t wbase = tile.begin + warp * 32; wbase < tile.end; wbase += SG_SIR_THREADS) {
+            const int32_t i = wbase + lane;
+            if (i < tile.end) {
+                a.cnt[i] = 0;
+                if (a.cls) {
+                    const int32_t st = sin[i];
+                    a.cls[i] = (uint8_t)(st == sg.ci ? 1 : st == sg.cs ? 0 : st == sg.cr ? 2 : 3);
+                }
+            }
+            if (a.cls && lane == 0) a.amask[wbase >> 5] = 0u;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_init_scatter_kernel(SgTickArgs a)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+        const SgTile tile = a.tiles[t];
+        const SgSeg &sg = a.segs[tile.seg];
+        const int32_t *__restrict__ sin = (const int32_t *)((sg.par0 & 1) ? a.buf1 : a.buf0);
+        for (int32_t wbase = tile.begin + warp * 32; wbase < tile.end; wbase += SG_SIR_THREADS) {
+            const int32_t i = wbase + lane;
+            unsigned m = __ballot_sync(FULL_MASK, i < tile.end && sin[i] == sg.ci);
+            while (m) {
+                const int l = __ffs(m) - 1;
+                m &= m - 1;
+                const int32_t j = wbase + l;
+                const int32_t b = __ldg(a.toff + j), e = __ldg(a.toff + j + 1);
+                for (int32_t p = b + lane; p < e; p += 32) {
+                    const int32_t k = __ldg(a.tidx + p);
+                    atomicAdd(a.cnt + k, 1);
+                    if (a.cls && a.cls[k] == 0) atomicOr(a.amask + (k >> 5), 1u << (k & 31));
+                }
+            }
+        }
+    }
+}
+
 // Warp-dense SIR-B draws. Lane l holds up to kCountPer susceptible agents; agent
 // q needs draws j = 0 .. k[q]-1 (salt 2 + j) until one is below beta. The warp
 // lays out the first min(k, kWarpDenseCap) draws of all its agents in one
@@ -914,6 +968,13 @@ static void launch_count_kernel(void (*k)(SgTickArgs), const SgTickArgs &a, int 
 cudaError_t sg_launch_sir_count_init(const SgTickArgs &a, int grid, cudaStream_t st)
 {
     sir_count_init_kernel<<<grid, SG_SIR_THREADS, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_launch_sir_count_init_scatter(const SgTickArgs &a, int grid, cudaStream_t st)
+{
+    sir_count_init_clear_kernel<<<grid, SG_SIR_THREADS, 0, st>>>(a);
+    sir_count_init_scatter_kernel<<<grid, SG_SIR_THREADS, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -710,6 +710,18 @@ static int grid_for(sg_engine *e, int32_t ntiles)
         ++e->last_launches;                                                                    \
     } while (0)
 
+// Infected-neighbour counts at the run start. A step over every agent counts by
+// scattering from the infected agents (two kernels; work = their degree sum),
+// any other by scanning its agents' rows.
+static cudaError_t launch_count_init(sg_engine *e, const SgStep *s, const SgTickArgs &a)
+{
+    if (s->begin == 0 && s->end == e->n) {
+        ++e->last_launches; // two kernels
+        return sg_launch_sir_count_init_scatter(a, grid_for(e, s->ntiles), e->stream);
+    }
+    return sg_launch_sir_count_init(a, grid_for(e, s->ntiles) + a.mega_blocks, e->stream);
+}
+
 // Enqueues nticks ticks (relative ticks 0..nticks-1) for the prepared steps.
 static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool stats_on,
                          bool capturing)
@@ -727,8 +739,7 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
             SG_CK(cudaMemsetAsync(e->fstats_init.p, 0, 4 * 8, e->stream));
             SG_CK(cudaMemsetAsync(e->fstats_delta.p, 0, (size_t)std::max(nticks, 1) * 32, e->stream));
         }
-        SG_PROF_LAUNCH("sir_count_init",
-                       sg_launch_sir_count_init(a, grid_for(e, s->ntiles) + a.mega_blocks, e->stream));
+        SG_PROF_LAUNCH("sir_count_init", launch_count_init(e, s, a));
         SG_PROF_LAUNCH("frontier_build", sg_launch_frontier_build(a, stats_on, grid_for(e, s->ntiles), e->stream));
         for (int32_t r = 0; r < nticks; ++r) {
             a.r = r;
@@ -747,8 +758,7 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
             SG_CK(cudaMemsetAsync(e->tick_changes.p, 0, (size_t)std::max(nticks, 1) * 4, e->stream));
             SG_CK(cudaMemsetAsync(e->tick_cand.p, 0, (size_t)std::max(nticks, 1) * 4, e->stream));
         }
-        SG_PROF_LAUNCH("sir_count_init",
-                       sg_launch_sir_count_init(a, grid_for(e, s->ntiles) + a.mega_blocks, e->stream));
+        SG_PROF_LAUNCH("sir_count_init", launch_count_init(e, s, a));
     }
     for (int32_t r = 0; r < nticks; ++r) {
         for (int32_t p : pl.copy_props) {

@@ -163,6 +163,11 @@ struct SgTickArgs {
 cudaError_t sg_launch_sir_pull(const SgTickArgs &a, int variant, bool stats, int grid,
                                cudaStream_t st);
 cudaError_t sg_launch_sir_count_init(const SgTickArgs &a, int grid, cudaStream_t st);
+// The same counts (and class bytes and activity bits) built by scattering from
+// the infected agents over the transpose rows: two kernels. Only for a step whose
+// tiles cover every agent of the graph with one segment; the grid takes no mega
+// blocks.
+cudaError_t sg_launch_sir_count_init_scatter(const SgTickArgs &a, int grid, cudaStream_t st);
 // inplace: the state buffer is read and written in place (buf0); only changed
 // agents are stored. Valid when the count step is the engine's only step, since
 // it reads nothing but the agent's own state and count.
