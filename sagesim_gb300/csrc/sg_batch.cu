@@ -154,7 +154,7 @@ bool SgPool::fits(int64_t n, int64_t nnz) const
 }
 
 int SgPool::place(const sg_scenario_desc &d, const int32_t *loff, const int32_t *lidx, const int32_t *state,
-                  const int64_t *llids, int32_t sid)
+                  const int64_t *llids, int32_t sid, bool check_on_device)
 {
     const int64_t n = d.n_agents, nnz = d.nnz;
     if (builtin == 0) builtin = d.builtin;
@@ -175,6 +175,20 @@ int SgPool::place(const sg_scenario_desc &d, const int32_t *loff, const int32_t 
     // local CSR copied as is, then shifted to pool slots on the device
     POOL_CK(cudaMemcpyAsync(off.as<int32_t>() + ab, loff, (size_t)(n + 1) * 4, cudaMemcpyHostToDevice, stream));
     if (nnz) POOL_CK(cudaMemcpyAsync(idx.as<int32_t>() + eb, lidx, (size_t)nnz * 4, cudaMemcpyHostToDevice, stream));
+    if (check_on_device) {
+        int32_t bad = 0;
+        POOL_CK(check_flag.reserve(4));
+        POOL_CK(cudaMemsetAsync(check_flag.p, 0, 4, stream));
+        POOL_CK(sg_launch_check_csr(off.as<int32_t>() + ab, n, idx.as<int32_t>() + eb, nnz, check_flag.as<int32_t>(),
+                                    stream));
+        POOL_CK(cudaMemcpyAsync(&bad, check_flag.p, 4, cudaMemcpyDeviceToHost, stream));
+        POOL_CK(cudaStreamSynchronize(stream));
+        if (bad) {
+            agents.give(ab, aslots);
+            if (nnz) edges.give(eb, nnz);
+            return fail(SG_ERR_BAD_CSR, bad == 1 ? "offsets decrease" : "an index is outside [0, n)");
+        }
+    }
     POOL_CK(sg_launch_offset_csr(off.as<int32_t>() + ab, n + 1, (int32_t)eb, idx.as<int32_t>() + eb, nnz,
                                  (int32_t)ab, stream));
     if (!all_symmetric) {

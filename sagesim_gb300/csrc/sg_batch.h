@@ -65,6 +65,7 @@ struct SgPool {
         rowsegs, nrowsegs, cls, amask, mrebuild, tick_changes;
     int32_t nchunks_cap = 0;
     SgDev snap_st[2], snap_cnt, snap_cls;
+    SgDev check_flag; // int32 result of sg_launch_check_csr
     bool any_lids = false, all_symmetric = true;
     int64_t seg_cap = 0, tile_cap = 0, mega_cap = 0;
 
@@ -101,9 +102,12 @@ struct SgPool {
     // Device arrays for the given capacities (contents of a smaller pool are
     // not kept: call before placing scenarios).
     int allocate(int64_t agent_cap, int64_t edge_cap, int64_t max_scen, bool transpose, bool lids);
-    // Validates and places one scenario (uploads CSR, state, lids).
+    // Places one scenario (uploads CSR, state, lids). check_on_device: the CSR
+    // has not been checked on the host; its offsets must start at 0 and end at
+    // nnz, and the rest (monotone offsets, indices in range) is checked on the
+    // device before anything is kept (SG_ERR_BAD_CSR, nothing placed).
     int place(const sg_scenario_desc &d, const int32_t *off, const int32_t *idx, const int32_t *state,
-              const int64_t *lids, int32_t sid);
+              const int64_t *lids, int32_t sid, bool check_on_device = false);
     void release(int32_t sid);
     bool fits(int64_t n, int64_t nnz) const;
     int rebuild_tables();

@@ -476,6 +476,20 @@ __global__ void offset_csr_kernel(int32_t *__restrict__ off, int64_t n1, int32_t
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz; k += stride) idx[k] += agent_base;
 }
 
+// flag = 1 when offsets decrease, 2 when an index is outside [0, n) (either
+// may win when both occur).
+__global__ void check_csr_kernel(const int32_t *__restrict__ off, int64_t n, const int32_t *__restrict__ idx,
+                                 int64_t nnz, int32_t *flag)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+        if (off[i + 1] < off[i]) *flag = 1;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz; k += stride) {
+        const int32_t v = idx[k];
+        if (v < 0 || (int64_t)v >= n) *flag = 2;
+    }
+}
+
 __global__ void copy_words_kernel(const uint32_t *__restrict__ src, uint32_t *__restrict__ dst,
                                   int64_t n)
 {
@@ -549,6 +563,17 @@ cudaError_t sg_launch_offset_csr(int32_t *off, int64_t n1, int32_t edge_base, in
     int64_t blocks = (work + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     offset_csr_kernel<<<(int)blocks, 256, 0, st>>>(off, n1, edge_base, idx, nnz, agent_base);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_launch_check_csr(const int32_t *off, int64_t n, const int32_t *idx, int64_t nnz, int32_t *flag,
+                                cudaStream_t st)
+{
+    const int64_t work = n > nnz ? n : nnz;
+    if (work <= 0) return cudaSuccess;
+    int64_t blocks = (work + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    check_csr_kernel<<<(int)blocks, 256, 0, st>>>(off, n, idx, nnz, flag);
     return cudaGetLastError();
 }
 

@@ -189,6 +189,11 @@ cudaError_t sg_launch_opinion_tables(double *radius, double *cosine, cudaStream_
 // scenario's local CSR into a pool).
 cudaError_t sg_launch_offset_csr(int32_t *off, int64_t n1, int32_t edge_base, int32_t *idx, int64_t nnz,
                                  int32_t agent_base, cudaStream_t st);
+// Checks a local CSR on the device (offsets[0] and offsets[n] checked by the
+// caller): *flag (zeroed by the caller) = 1 if the offsets decrease, 2 if an
+// index is outside [0, n).
+cudaError_t sg_launch_check_csr(const int32_t *off, int64_t n, const int32_t *idx, int64_t nnz, int32_t *flag,
+                                cudaStream_t st);
 // Copies [begin, end) of `words` 32-bit words from src to dst (write-back of
 // agents outside a step's range).
 cudaError_t sg_launch_copy_words(const uint32_t *src, uint32_t *dst, int64_t n, cudaStream_t st);

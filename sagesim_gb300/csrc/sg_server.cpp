@@ -160,14 +160,42 @@ int sg_server_submit(sg_server *s, const sg_scenario_desc *d, int64_t *rid)
     if (d->builtin != s->cfg.builtin) return s->pool.fail(SG_ERR_INVALID, "request builtin differs from the server's");
     if (!(d->flags & SG_GRAPH_SYMMETRIC)) return s->pool.fail(SG_ERR_INVALID, "the server takes symmetric (undirected) graphs");
     if (d->horizon < 0) return s->pool.fail(SG_ERR_INVALID, "horizon < 0");
-    std::string why = sg_check_csr(d->offsets, d->n_agents, d->indices, d->nnz);
-    if (!why.empty()) return s->pool.fail(SG_ERR_BAD_CSR, why);
+    if (d->n_agents < 0 || d->nnz < 0 || !d->offsets || (d->nnz > 0 && !d->indices))
+        return s->pool.fail(SG_ERR_INVALID, "bad CSR sizes or NULL arrays");
     if (!d->state && d->n_agents > 0) return s->pool.fail(SG_ERR_INVALID, "state is NULL");
     const int64_t bytes = sg_pool_scenario_bytes(d->n_agents, d->nnz, false, false);
     if (bytes > s->cfg.budget_bytes || d->n_agents + 1 > s->cfg.agent_slots || d->nnz > s->cfg.edge_slots)
         return s->pool.fail(SG_ERR_BUDGET, "request needs " + std::to_string((long long)bytes) +
                                                " bytes / slots beyond the server's budget or pool");
     if (d->lids) return s->pool.fail(SG_ERR_INVALID, "the server keys the RNG on local agent indices");
+    if (d->offsets[0] != 0 || d->offsets[d->n_agents] != d->nnz)
+        return s->pool.fail(SG_ERR_BAD_CSR, "offsets must start at 0 and end at nnz");
+    // Nothing queued ahead and room now: placed on the device at once, straight
+    // from the caller's arrays, with the CSR checked there (no host pass over
+    // the edges). Otherwise the request is checked and copied on the host.
+    if (s->queue.empty() && s->resident_bytes + bytes <= s->cfg.budget_bytes &&
+        s->pool.fits(d->n_agents, d->nnz)) {
+        const int32_t sid = s->next_sid++;
+        const int rc = s->pool.place(*d, d->offsets, d->indices, d->state, nullptr, sid, true);
+        if (rc == SG_OK) {
+            auto r = std::make_unique<Request>();
+            r->rid = s->next_rid++;
+            r->d = *d;
+            r->d.offsets = r->d.indices = r->d.state = nullptr;
+            r->d.lids = nullptr;
+            r->bytes = bytes;
+            r->status = SG_REQ_RUNNING;
+            *rid = r->rid;
+            s->rid_sid[r->rid] = sid;
+            s->resident_bytes += bytes;
+            s->reqs[r->rid] = std::move(r);
+            return SG_OK;
+        }
+        if (rc != SG_ERR_BUDGET) return rc; // SG_ERR_BAD_CSR from the device check, or a CUDA error
+        // fragmented pool: queue it
+    }
+    std::string why = sg_check_csr(d->offsets, d->n_agents, d->indices, d->nnz);
+    if (!why.empty()) return s->pool.fail(SG_ERR_BAD_CSR, why);
     auto r = std::make_unique<Request>();
     r->rid = s->next_rid++;
     r->d = *d;

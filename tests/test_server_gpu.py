@@ -49,7 +49,7 @@ def test_poll_and_take_result():
     r = requests(1, 13)[0]
     with Server(budget_bytes=1 << 30, agent_slots=1_000_000, edge_slots=10_000_000) as srv:
         rid = srv.submit(**r)
-        assert srv.poll(rid)[0] == 0  # queued
+        assert srv.poll(rid) == (1, 0)  # room at once: placed on the device, running
         srv.step(5)
         st, tk = srv.poll(rid)
         assert st == 1 and tk == 5
@@ -59,3 +59,37 @@ def test_poll_and_take_result():
         assert np.array_equal(got, standalone(r, "B", r["horizon"]))
         with pytest.raises(SageSimError):
             srv.poll(rid)
+
+
+def est_bytes(r):
+    """About the server's footprint of a request (22 B per agent slot, 4 B per
+    CSR entry, tile and segment tables)."""
+    n, nnz = r["offsets"].size - 1, r["indices"].size
+    return ((n + 32) & ~31) * 22 + nnz * 4 + ((n + 2047) // 2048 + 1) * 20 + 256
+
+
+def test_bad_csr_is_refused_on_both_submission_paths():
+    """Placed at once (CSR checked on the device) or queued behind a request
+    that fills the budget (checked on the host): a bad CSR is SG_ERR_BAD_CSR,
+    nothing of it stays, and later requests run as they would alone."""
+    good, other = requests(2, 14)
+    bad_index = dict(other, indices=other["indices"].copy())
+    bad_index["indices"][-1] = other["offsets"].size - 1 + 5
+    bad_order = dict(other, offsets=other["offsets"].copy())
+    bad_order["offsets"][3] = bad_order["offsets"][4] + 1
+    for placed_at_once in (True, False):
+        budget = (1 << 30) if placed_at_once else est_bytes(good) + est_bytes(other) // 2
+        with Server(budget_bytes=budget, agent_slots=1_000_000, edge_slots=10_000_000) as srv:
+            if not placed_at_once:
+                first = srv.submit(**good)
+                assert srv.poll(first)[0] == 1
+            for bad in (bad_index, bad_order):
+                with pytest.raises(SageSimError, match="BAD_CSR"):
+                    srv.submit(**bad)
+            assert srv.counts()["queued"] == 0
+            rid = srv.submit(**other)
+            if not placed_at_once:
+                assert srv.poll(rid)[0] == 0  # queued behind the first
+            while srv.poll(rid)[0] != 2:
+                srv.step(16)
+            assert np.array_equal(srv.take_result(rid), standalone(other, "B", other["horizon"]))
