@@ -301,7 +301,9 @@ def serving_section(stream, device=0, n_requests=100, n_graphs=24):
     n log-uniform in [1e4, 5e6], BA or ER with mean degree 4..16, horizons
     U{50..365}, 150 GB admission budget. Graph structures come from a pool of
     n_graphs generated graphs; every request has its own seed, beta, gamma,
-    initial infections and horizon."""
+    initial infections and horizon. The Poisson stream gives the latencies (its
+    throughput is bounded by the arrival rate); the same requests all arriving
+    at once give the served form's capacity (burst_*)."""
     import torch
 
     from sagesim_gb300 import Engine, graphs
@@ -330,6 +332,11 @@ def serving_section(stream, device=0, n_requests=100, n_graphs=24):
                      max_resident=4096, variant="B", device=device, stream=stream.cuda_stream)
         out = serve_stream(srv, reqs, arrivals, chunk=8)
         srv.close()
+        # capacity: the same requests all arriving at once
+        srv = Server(budget_bytes=150 * 10**9, agent_slots=400_000_000, edge_slots=2_100_000_000,
+                     max_resident=4096, variant="B", device=device, stream=stream.cuda_stream)
+        burst = serve_stream(srv, reqs, np.zeros(n_requests), chunk=8, keep_results=False)
+        srv.close()
         # plain sequential: each request alone on the plain engine (device time)
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         plain_ms, mismatches, checked = 0.0, 0, 0
@@ -355,6 +362,10 @@ def serving_section(stream, device=0, n_requests=100, n_graphs=24):
                         % (n_requests, n_graphs),
             "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
             "served_agent_ticks_per_s": agent_ticks / out["wall_s"], "wall_s": out["wall_s"],
+            "arrival_span_s": float(arrivals[-1]), "submit_s": out["submit_s"], "step_s": out["step_s"],
+            "burst_agent_ticks_per_s": burst["agent_ticks"] / burst["wall_s"], "burst_wall_s": burst["wall_s"],
+            "burst_p50_latency_s": float(np.percentile(burst["latency_s"], 50)),
+            "burst_p99_latency_s": float(np.percentile(burst["latency_s"], 99)),
             "plain_sequential_agent_ticks_per_s": agent_ticks / (plain_ms / 1e3),
             "bit_exact_requests": checked - mismatches, "requests": n_requests}
 

@@ -88,7 +88,8 @@ class Server:
 def serve_stream(server, requests, arrivals, chunk=8, keep_results=True, clock=time.perf_counter):
     """Submits requests[i] (dict of Server.submit kwargs) at arrivals[i] seconds
     after the start, steps the server by `chunk` ticks while work remains, and
-    returns per-request latency (completion - arrival, seconds), results and totals."""
+    returns per-request latency (completion - arrival, seconds), results and totals
+    (with the host time spent in submit and in step)."""
     order = np.argsort(arrivals, kind="stable")
     t0 = clock()
     rid_of, req_of = {}, {}
@@ -97,11 +98,14 @@ def serve_stream(server, requests, arrivals, chunk=8, keep_results=True, clock=t
     nxt = 0
     pending = 0
     agent_ticks = 0
+    t_submit = t_step = 0.0
     while nxt < len(order) or pending:
         now = clock() - t0
         while nxt < len(order) and arrivals[order[nxt]] <= now:
             i = int(order[nxt])
+            ts = clock()
             rid = server.submit(**requests[i])
+            t_submit += clock() - ts
             rid_of[i] = rid
             req_of[rid] = i
             pending += 1
@@ -112,7 +116,9 @@ def serve_stream(server, requests, arrivals, chunk=8, keep_results=True, clock=t
             if wait > 0:
                 time.sleep(min(wait, 0.01))
             continue
+        ts = clock()
         finished = server.step(chunk)
+        t_step += clock() - ts
         if finished:
             tnow = clock() - t0
             for rid in list(req_of):
@@ -127,4 +133,5 @@ def serve_stream(server, requests, arrivals, chunk=8, keep_results=True, clock=t
                     pending -= 1
     wall = clock() - t0
     lat = np.array([done_at[i] - arrivals[i] for i in range(len(requests))])
-    return {"latency_s": lat, "results": results, "wall_s": wall, "agent_ticks": agent_ticks}
+    return {"latency_s": lat, "results": results, "wall_s": wall, "agent_ticks": agent_ticks,
+            "submit_s": t_submit, "step_s": t_step}
