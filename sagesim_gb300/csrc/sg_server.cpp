@@ -267,7 +267,7 @@ int sg_server_set_tune(sg_server *s, const sg_tune *t)
     if (!s || !t) return SG_ERR_INVALID;
     if (t->strategy != SG_SIR_PULL && t->strategy != SG_SIR_COUNT) return s->pool.fail(SG_ERR_INVALID, "bad strategy");
     if (t->blocks_per_sm < 1 || t->blocks_per_sm > 32 || t->thread_row < 1 || t->mega_row < 512 ||
-        t->count_flavour < 0 || t->count_flavour > 7)
+        t->count_flavour < 0 || t->count_flavour > SG_FLAVOUR_MAX)
         return s->pool.fail(SG_ERR_INVALID, "tune parameters out of range");
     const bool mega_changed = t->mega_row != s->pool.tune.mega_row;
     s->pool.tune = *t;

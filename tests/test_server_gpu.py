@@ -48,6 +48,9 @@ def test_request_over_budget_is_refused():
 def test_poll_and_take_result():
     r = requests(1, 13)[0]
     with Server(budget_bytes=1 << 30, agent_slots=1_000_000, edge_slots=10_000_000) as srv:
+        srv.set_tune()  # the defaults (class sweep + hybrid step) are accepted
+        with pytest.raises(SageSimError):
+            srv.set_tune(count_flavour=512)
         rid = srv.submit(**r)
         assert srv.poll(rid) == (1, 0)  # room at once: placed on the device, running
         srv.step(5)
