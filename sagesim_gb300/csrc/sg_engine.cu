@@ -58,6 +58,7 @@ struct sg_engine {
     bool own_stream = false;
     int sm_count = 152;
     size_t l2_window_max = 0; // largest access-policy window (bytes), 0 = unsupported
+    size_t l2_limit_bytes = 0; // persisting-line capacity set for this context
     std::string err;
 
     int64_t n = -1, nnz = 0;
@@ -787,6 +788,11 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
             } else if (s->kind == SG_BUILTIN_OPINION) {
                 a.bm_radius = e->bm_ready ? e->bm_radius.as<double>() : nullptr;
                 a.bm_cos = e->bm_ready ? e->bm_cos.as<double>() : nullptr;
+                if (e->bm_ready && e->l2_limit_bytes) {
+                    a.l2_win = a.bm_cos;
+                    a.l2_win_bytes = std::min(e->l2_window_max, (size_t)SG_BOX_MULLER_SIZE * sizeof(double));
+                    a.l2_win_hit = (float)std::min(1.0, (double)e->l2_limit_bytes / (double)a.l2_win_bytes);
+                }
                 SG_PROF_LAUNCH("opinion", sg_launch_opinion(a, grid, e->stream, s->host_seg.width));
             } else {
                 sg_step_args L{};
@@ -898,7 +904,15 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
     }
     if (e->cls_on && e->l2_window_max && !e->l2_limit_set) {
         // persisting-line capacity of this context (ends with it) for the counts' window
-        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, std::min(e->l2_window_max, (size_t)e->n * 4));
+        e->l2_limit_bytes = std::min(e->l2_window_max, (size_t)e->n * 4);
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, e->l2_limit_bytes);
+        (void)cudaGetLastError();
+        e->l2_limit_set = true;
+    }
+    if (e->bm_ready && e->l2_window_max && !e->l2_limit_set) {
+        // the opinion step's cosine table (64 MiB, read at random) as persisting lines
+        e->l2_limit_bytes = std::min(e->l2_window_max, (size_t)SG_BOX_MULLER_SIZE * sizeof(double));
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, e->l2_limit_bytes);
         (void)cudaGetLastError();
         e->l2_limit_set = true;
     }

@@ -458,7 +458,7 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) opinion_kernel(SgTickArgs a)
             const uint32_t k1 = sg_philox_k23(c0b + 1u, lid, sg.key);
             const uint32_t k2 = sg_philox_k23(c0b + 1u + kNormalSalt2, lid, sg.key);
             const double r = a.bm_radius ? __ldcs(a.bm_radius + k1) : bm_radius(k1);
-            const double c = a.bm_cos ? __ldcs(a.bm_cos + k2) : bm_cos(k2);
+            const double c = a.bm_cos ? (a.l2_win ? __ldg(a.bm_cos + k2) : __ldcs(a.bm_cos + k2)) : bm_cos(k2);
             const double z = __dmul_rn(r, c);
             double y = __dadd_rn((double)x, __dmul_rn(sg.sigma, z));
             if (y < 0.0) y = 0.0;
@@ -548,11 +548,25 @@ cudaError_t sg_launch_opinion_tables(double *radius, double *cosine, cudaStream_
 // vector-load path).
 cudaError_t sg_launch_opinion(const SgTickArgs &a, int grid, cudaStream_t st, int width)
 {
-    if (width == 8)
-        opinion_kernel<8><<<grid, SG_SIR_THREADS, 0, st>>>(a);
-    else
-        opinion_kernel<0><<<grid, SG_SIR_THREADS, 0, st>>>(a);
-    return cudaGetLastError();
+    void (*k)(SgTickArgs) = width == 8 ? opinion_kernel<8> : opinion_kernel<0>;
+    if (!a.l2_win) {
+        k<<<grid, SG_SIR_THREADS, 0, st>>>(a);
+        return cudaGetLastError();
+    }
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(SG_SIR_THREADS);
+    cfg.stream = st;
+    cudaLaunchAttribute at{};
+    at.id = cudaLaunchAttributeAccessPolicyWindow;
+    at.val.accessPolicyWindow.base_ptr = const_cast<void *>(a.l2_win);
+    at.val.accessPolicyWindow.num_bytes = a.l2_win_bytes;
+    at.val.accessPolicyWindow.hitRatio = a.l2_win_hit;
+    at.val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    at.val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    cfg.attrs = &at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, a);
 }
 
 cudaError_t sg_launch_offset_csr(int32_t *off, int64_t n1, int32_t edge_base, int32_t *idx, int64_t nnz,

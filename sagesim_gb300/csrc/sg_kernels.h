@@ -142,6 +142,9 @@ struct SgTickArgs {
                             // (an access-policy window on the count kernels); 0 = none
     const double *bm_radius; // opinion: NULL, or the 2^23-entry Box-Muller tables of
     const double *bm_cos;    // sg_launch_opinion_tables
+    const void *l2_win;     // opinion: NULL, or an access-policy window (persisting lines)
+    size_t l2_win_bytes;    // over l2_win_bytes from l2_win, a fraction l2_win_hit of its
+    float l2_win_hit;       // lines kept (the cosine table, read at random)
     int32_t hybrid_rise;    // hybrid count step (0 = off): tick r > 1 runs the loop form
     int32_t hybrid_fall;    // when tick r - 1 recorded more than hybrid_rise changes and
                             // no fewer than tick r - 2 (epidemic growing), or more than
