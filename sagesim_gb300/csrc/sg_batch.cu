@@ -10,6 +10,7 @@
 #include <cstring>
 #include <limits>
 #include <memory>
+#include <thread>
 
 #include "sg_batch.h"
 #include "sg_philox.h"
@@ -110,10 +111,58 @@ void SgPool::destroy()
 {
     cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
+    for (int h = 0; h < 2; ++h) {
+        if (stage[h]) cudaFreeHost(stage[h]);
+        if (stage_ev[h]) cudaEventDestroy(stage_ev[h]);
+        stage[h] = nullptr;
+        stage_ev[h] = nullptr;
+    }
     if (graph) cudaGraphExecDestroy(graph);
     graph = nullptr;
     if (own_stream && stream) cudaStreamDestroy(stream);
     stream = nullptr;
+}
+
+namespace {
+constexpr size_t kStageBytes = (size_t)32 << 20;
+constexpr size_t kStageMin = (size_t)4 << 20; // smaller uploads: one direct copy
+
+// dst[0, len) = src[0, len) with up to `threads` host threads.
+void parallel_copy(char *dst, const char *src, size_t len, unsigned threads)
+{
+    const size_t part = ((len + threads - 1) / threads + 63) & ~(size_t)63;
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < threads && (size_t)t * part < len; ++t) {
+        const size_t b = (size_t)t * part, n = std::min(part, len - b);
+        pool.emplace_back([=] { memcpy(dst + b, src + b, n); });
+    }
+    memcpy(dst, src, std::min(part, len));
+    for (auto &th : pool) th.join();
+}
+} // namespace
+
+int SgPool::upload(void *dst, const void *src, size_t bytes)
+{
+    if (bytes < kStageMin) {
+        POOL_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream));
+        return SG_OK;
+    }
+    if (!stage[0]) {
+        for (int h = 0; h < 2; ++h) {
+            POOL_CK(cudaHostAlloc(&stage[h], kStageBytes, cudaHostAllocDefault));
+            POOL_CK(cudaEventCreateWithFlags(&stage_ev[h], cudaEventDisableTiming));
+        }
+    }
+    const unsigned threads = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+    int h = 0;
+    for (size_t pos = 0; pos < bytes; pos += kStageBytes, h ^= 1) {
+        const size_t len = std::min(kStageBytes, bytes - pos);
+        POOL_CK(cudaEventSynchronize(stage_ev[h])); // this buffer's previous copy has left
+        parallel_copy((char *)stage[h], (const char *)src + pos, len, threads);
+        POOL_CK(cudaMemcpyAsync((char *)dst + pos, stage[h], len, cudaMemcpyHostToDevice, stream));
+        POOL_CK(cudaEventRecord(stage_ev[h], stream));
+    }
+    return SG_OK;
 }
 
 int SgPool::allocate(int64_t acap, int64_t ecap, int64_t max_scen, bool transpose, bool with_lids)
@@ -173,8 +222,13 @@ int SgPool::place(const sg_scenario_desc &d, const int32_t *loff, const int32_t 
     }
     POOL_CK(cudaSetDevice(device));
     // local CSR copied as is, then shifted to pool slots on the device
-    POOL_CK(cudaMemcpyAsync(off.as<int32_t>() + ab, loff, (size_t)(n + 1) * 4, cudaMemcpyHostToDevice, stream));
-    if (nnz) POOL_CK(cudaMemcpyAsync(idx.as<int32_t>() + eb, lidx, (size_t)nnz * 4, cudaMemcpyHostToDevice, stream));
+    int urc = upload(off.as<int32_t>() + ab, loff, (size_t)(n + 1) * 4);
+    if (!urc && nnz) urc = upload(idx.as<int32_t>() + eb, lidx, (size_t)nnz * 4);
+    if (urc) {
+        agents.give(ab, aslots);
+        if (nnz) edges.give(eb, nnz);
+        return urc;
+    }
     if (check_on_device) {
         int32_t bad = 0;
         POOL_CK(check_flag.reserve(4));
@@ -204,7 +258,14 @@ int SgPool::place(const sg_scenario_desc &d, const int32_t *loff, const int32_t 
         POOL_CK(cudaMemcpyAsync(toff.as<int32_t>() + ab, tcount.data(), (size_t)(n + 1) * 4, cudaMemcpyHostToDevice, stream));
         if (nnz) POOL_CK(cudaMemcpyAsync(tidx.as<int32_t>() + eb, t.data(), (size_t)nnz * 4, cudaMemcpyHostToDevice, stream));
     }
-    POOL_CK(cudaMemcpyAsync(st[0].as<int32_t>() + ab, state, (size_t)n * 4, cudaMemcpyHostToDevice, stream));
+    {
+        const int rc = upload(st[0].as<int32_t>() + ab, state, (size_t)n * 4);
+        if (rc) {
+            agents.give(ab, aslots);
+            if (nnz) edges.give(eb, nnz);
+            return rc;
+        }
+    }
     SgPoolScen s;
     s.sid = sid;
     s.n = n;

@@ -66,6 +66,12 @@ struct SgPool {
     int32_t nchunks_cap = 0;
     SgDev snap_st[2], snap_cnt, snap_cls;
     SgDev check_flag; // int32 result of sg_launch_check_csr
+    // Large host -> device uploads go through two pinned staging buffers that
+    // several host threads fill while the other one is in flight; a copy from
+    // pageable memory runs far below the link's bandwidth.
+    void *stage[2] = {nullptr, nullptr};
+    cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+    int upload(void *dst, const void *src, size_t bytes);
     bool any_lids = false, all_symmetric = true;
     int64_t seg_cap = 0, tile_cap = 0, mega_cap = 0;
 
