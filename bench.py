@@ -523,7 +523,8 @@ def sweep(args):
         eng.snapshot()
         ref = None
         for bps in (8, 16):
-            for fl in (0, 4, 5, 16, 24, 16 | 256 | 4, 16 | 256 | 5, 16 | 256):
+            for fl in (0, 2, 3, 4, 5, 16, 24, 16 | 256, 16 | 256 | 2, 16 | 256 | 3, 16 | 256 | 4, 16 | 256 | 5,
+                       16 | 256 | 6):
                 eng.set_tune(blocks_per_sm=bps, count_flavour=fl)
                 for _ in range(2):
                     eng.restore()

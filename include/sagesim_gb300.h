@@ -144,7 +144,8 @@ typedef struct sg_tune {
                                /* 256 = with 16: hybrid, the loop form of bits   */
                                /*      0-2 in busy ticks (decided on the GPU;    */
                                /*      graphs of 24+ tiles per SM, or with 32)   */
-                               /* default 272 (class sweep + hybrid)             */
+                               /* default 278: class sweep + hybrid whose loop   */
+                               /*      form has warp-dense draws and lazy loads  */
     double us_per_tick;        /* measured by sg_batch_tune (output)             */
 } sg_tune;
 

@@ -91,7 +91,8 @@ struct sg_engine {
 
     SgProfiler prof;
     int hub_deg = 32;
-    sg_tune tune{SG_SIR_COUNT, 16, 32, 2048, SG_FLAVOUR_SWEEP | SG_FLAVOUR_HYBRID, 0.0};
+    sg_tune tune{SG_SIR_COUNT, 16, 32, 2048,
+                 SG_FLAVOUR_SWEEP | SG_FLAVOUR_HYBRID | SG_FLAVOUR_DENSE | SG_FLAVOUR_LAZY, 0.0};
     int32_t last_nticks = 0;
     int64_t last_launches = 0; // kernels launched by the last enqueued run
 

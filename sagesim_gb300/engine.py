@@ -221,7 +221,7 @@ class Engine:
     def restore(self):
         self._ck(self._lib.sg_restore(self._h))
 
-    def set_tune(self, blocks_per_sm=16, thread_row=32, mega_row=2048, count_flavour=272):
+    def set_tune(self, blocks_per_sm=16, thread_row=32, mega_row=2048, count_flavour=278):
         """Launch configuration of the SIR kernels (results are identical for all)."""
         t = N.Tune(N.SG_SIR_COUNT, blocks_per_sm, thread_row, mega_row, count_flavour, 0.0)
         self._ck(self._lib.sg_engine_set_tune(self._h, ctypes.byref(t)))

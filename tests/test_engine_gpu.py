@@ -82,7 +82,8 @@ def test_sir_matches_oracle_every_tick(variant, strategy, kind):
             st = ref
 
 
-COUNT_FLAVOURS = list(range(8)) + [8, 12, 16, 24, 48, 56, 63, 48 | 64, 48 | 128, 56 | 192, 48 | 256 | 4, 48 | 256 | 1, 16 | 256]
+COUNT_FLAVOURS = list(range(8)) + [8, 12, 16, 24, 48, 56, 63, 48 | 64, 48 | 128, 56 | 192, 48 | 256 | 4, 48 | 256 | 1,
+                                   16 | 256, 48 | 256 | 6, 16 | 256 | 6]
 
 
 @pytest.mark.parametrize("flavour", COUNT_FLAVOURS)
@@ -108,7 +109,7 @@ def test_count_step_flavours_identical(flavour, variant):
     assert np.array_equal(got, ref)
 
 
-@pytest.mark.parametrize("flavour", [0, 16, 48, 48 | 64, 48 | 128, 48 | 256 | 4, 48 | 256 | 3])
+@pytest.mark.parametrize("flavour", [0, 16, 48, 48 | 64, 48 | 128, 48 | 256 | 4, 48 | 256 | 3, 48 | 256 | 6])
 @pytest.mark.parametrize("variant", ["A", "B"])
 def test_count_dense_graph_with_statistics(flavour, variant):
     """A dense graph with many infected neighbours per agent and a small beta
