@@ -3,7 +3,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle
-from sagesim_gb300 import Engine, graphs
+from sagesim_gb300 import Engine, SageSimError, graphs
 
 pytestmark = pytest.mark.gpu
 
@@ -151,3 +151,49 @@ def test_class_sweep_statistics_on_power_law_graph(variant, wpt_bits):
     ref, rstats, _ = oracle.sir_run(1 if variant == "A" else 2, off, idx, st0, 5, 0, 60, 0.2, 0.1)
     assert np.array_equal(got, ref)
     assert np.array_equal(stats, rstats)
+
+
+def test_array_rows_bounds_and_snapshot():
+    """An engine array (breed-local array storage) with its own row count: a
+    compiled step reads tick-start values (double-buffered), reads 0 and drops
+    writes outside the array, and get/set_property, snapshot and restore address
+    its rows."""
+    n, rows = 100, 40
+    off, idx = graphs.erdos_renyi(n, 0.05, 3)
+    with Engine() as e:
+        e.set_graph(off, idx, symmetric=True)
+        p = e.add_property("state", np.int32, init=np.zeros(n, dtype=np.int32))
+        arr = e.add_array("sgbla_h", np.float32, 3, rows)
+        imap = np.where(np.arange(n) < rows, np.arange(n), -1).astype(np.int32)
+        pi = e.add_property("sgbla_h_idx", np.int32, init=imap, double_buffered=False)
+        src = ("#define PROP_state %d\n#define PROP_sgbla_h %d\n#define PROP_sgbla_h_idx %d\n" % (p, arr, pi)) + """
+__device__ void f(const sg_ctx &ctx, int i)
+{
+    const long long row = ctx.i32(PROP_sgbla_h_idx, i);
+    const float v = ctx.arr_f32(PROP_sgbla_h, row, 0) + ctx.arr_f32(PROP_sgbla_h, row, 7) + 1.0f;
+    ctx.set_arr_f32(PROP_sgbla_h, row, v, 0);
+    ctx.set_arr_f32(PROP_sgbla_h, row, (float)ctx.tick, 2);
+    ctx.set_arr_f32(PROP_sgbla_h, row + 1000, 5.0f, 0);
+    ctx.set_arr_f32(PROP_sgbla_h, row, 9.0f, 3);
+    ctx.set_i32(PROP_state, i, ctx.i32(PROP_state, i) + 1);
+}
+"""
+        e.compile_step(src, "f", [arr, p])
+        e.run(0, 5, stats=False)
+        h = e.get_property(arr)
+        assert h.shape == (rows, 3)
+        assert (h[:, 0] == 5).all() and (h[:, 1] == 0).all() and (h[:, 2] == 4).all()
+        assert (e.get_property(p) == 5).all()
+        assert np.array_equal(e.get_property(arr, first=10, count=5), h[10:15])
+        e.snapshot()
+        e.run(5, 2, stats=False)
+        assert (e.get_property(arr)[:, 0] == 7).all()
+        e.restore()
+        assert (e.get_property(arr)[:, 0] == 5).all()
+        e.set_property(arr, np.ones((2, 3), dtype=np.float32), first=rows - 2)
+        assert (e.get_property(arr)[rows - 2:] == 1).all()
+        with pytest.raises(SageSimError):
+            e.get_property(arr, first=rows - 1, count=2)
+        a2 = e.add_array("a2", np.int32, 1, rows)
+        with pytest.raises(SageSimError, match="agent property"):
+            e.add_sir(a2, 0.1, 0.1)  # an array is not an agent property
