@@ -26,12 +26,16 @@ void sg_set_thread_error(const std::string &msg); // sg_engine.cu
 namespace {
 constexpr int32_t kLongRowFloor = 512; // rows kept as mega candidates (smallest tunable mega_row)
 // count-step flavours the autotuner times: loop form (4 or 8 agents per thread,
-// eager or lazy loads) and class sweep with the load-balanced scatter, and two
-// of them with the lane-per-row scatter
+// eager or lazy loads, per-lane or warp-dense draws) and class sweep with the
+// load-balanced scatter (alone or in the hybrid), and two of them with the
+// lane-per-row scatter
 constexpr int32_t kCountFlavourCands[] = {0,
                                           1,
                                           4,
                                           5,
+                                          SG_FLAVOUR_DENSE,
+                                          SG_FLAVOUR_DENSE | SG_FLAVOUR_LAZY,
+                                          SG_FLAVOUR_SWEEP | SG_FLAVOUR_HYBRID | SG_FLAVOUR_DENSE | SG_FLAVOUR_LAZY,
                                           SG_FLAVOUR_SWEEP,
                                           SG_FLAVOUR_SWEEP | SG_FLAVOUR_FORCE,
                                           SG_FLAVOUR_SWEEP | SG_FLAVOUR_HYBRID,

@@ -61,7 +61,8 @@ def test_batch_scenarios_match_standalone(strategy, variant):
             assert np.array_equal(b.get_state(sid), want), "scenario %d" % sid
 
 
-@pytest.mark.parametrize("flavours", [(48, 0, 48 | 64), (0, 48 | 128, 4), (56, 5, 49), (16, 0, 16), (48 | 256 | 4, 0, 48 | 256)])
+@pytest.mark.parametrize("flavours", [(48, 0, 48 | 64), (0, 48 | 128, 4), (56, 5, 49), (16, 0, 16), (48 | 256 | 4, 0, 48 | 256),
+                                      (6, 48 | 256 | 6, 2)])
 def test_batch_count_flavours_switch_between_runs(flavours):
     """Class bytes are kept by every count-strategy kernel and the activity bits
     are rebuilt at the start of every run, so the class sweep can take over from
