@@ -43,7 +43,7 @@ SEED = 1
 #       --clock-control none --csv --log-file dram.csv python bench.py --profile-case
 # keyed by (strategy, agents, kernel); the count step is the sum of both hybrid kernels
 # per tick. Re-measure when a kernel changes.
-MEASURED_TRAFFIC = {("count", 10_000_000, "sir_count_step"): 56.975e6}
+MEASURED_TRAFFIC = {("count", 10_000_000, "sir_count_step"): 56.892e6}
 PARTS = 64
 CODES = (1, 2, 3)
 
