@@ -3,7 +3,8 @@
 Public interface of sagesim/model.py:355-998 for the per-tick agent step:
 register_breed, create_agent_of_breed, register/set/get_global_property,
 set_seed, set_agent_logical_id, setup, simulate, get/set_agent_property_value,
-get_breed_data, reset. setup() does what the reference's setup() plus its
+get_breed_data, get_breed_agent_ids, register/get_breed_local_array,
+set_property_neighbor_visible, reset, save, load. setup() does what the reference's setup() plus its
 first-simulate buffer build do (sagesim/model.py:682-886, 1020-1274): agents
 are stably sorted by breed (sagesim/agent.py:438-473), the NetworkSpace
 becomes a device CSR of buffer indices, every property a structure-of-arrays
@@ -14,6 +15,7 @@ engine over that breed's index range. simulate() then runs the ticks on the
 GPU with the tick counter continuing across calls (model.py:1576).
 """
 import math
+import pickle
 import time
 
 import numpy as np
@@ -49,6 +51,7 @@ class Model:
         self.tick = 0
         self._engine = None
         self._breed_local_arrays = []
+        self._neighbor_visible_override = {}
         self._tick_timings = []
 
     # ---- properties of the model ------------------------------------------------
@@ -421,6 +424,56 @@ class Model:
         v = self._engine.get_property(self._pid[property_name], b, e - b)
         return v.tolist()
 
+    def get_breed_agent_ids(self, breed_name, local=False):
+        """sagesim/model.py:492-515: the breed's agent ids in buffer order, as
+        the float32 values the reference keeps them in."""
+        bidx = self._agent_factory._breeds[breed_name]._breedidx
+        if not self._is_setup:
+            raise RuntimeError("call setup() before get_breed_agent_ids()")
+        b, e = self._breed_ranges.get(bidx, (0, 0))
+        return self._order[b:e].astype(np.float32)
+
+    def set_property_neighbor_visible(self, property_name, visible):
+        """sagesim/model.py:398-409: the flag only selects what crosses ranks in
+        the reference's ghost exchange; one GPU holds every agent, so it is
+        recorded and changes nothing here."""
+        if self._is_setup:
+            raise RuntimeError("Cannot change neighbor_visible after setup()")
+        af = self._agent_factory
+        if property_name not in af._property_name_2_index:
+            raise ValueError("Unknown property: %s" % property_name)
+        self._neighbor_visible_override[property_name] = bool(visible)
+
+    def _sync_to_host(self):
+        """Copies the device values of every property into the host store."""
+        af = self._agent_factory
+        for name in self._props:
+            vals = self.get_property_array(name)
+            col = af.column(name)
+            for a in range(len(col)):
+                col[a] = vals[a].tolist() if vals.ndim > 1 else vals[a].item()
+
+    def __getstate__(self):
+        # the device engine is not picklable: its property values go to the
+        # host store and the next simulate() builds a new engine from them
+        if self._engine is not None:
+            self._sync_to_host()
+        state = self.__dict__.copy()
+        state["_engine"] = None
+        return state
+
+    def save(self, app, fpath):
+        """sagesim/model.py:1288-1298: pickles `app` (a Model) to fpath. Property
+        values and the tick are kept; breed-local arrays restart from zeros
+        when the loaded model next runs."""
+        with open(fpath, "wb") as fout:
+            pickle.dump(app, fout)
+
+    def load(self, fpath):
+        """sagesim/model.py:1300-1309: the model pickled at fpath."""
+        with open(fpath, "rb") as fin:
+            return pickle.load(fin)
+
     def get_property_array(self, property_name):
         """All agents' values by agent id as a numpy array (one device copy)."""
         v = self._engine.get_property(self._pid[property_name])
@@ -433,12 +486,7 @@ class Model:
         host store, device buffers freed (rebuilt on the next simulate)."""
         self.tick = 0
         if self._engine is not None:
-            af = self._agent_factory
-            for name in self._props:
-                vals = self.get_property_array(name)
-                col = af.column(name)
-                for a in range(len(col)):
-                    col[a] = vals[a].tolist() if vals.ndim > 1 else vals[a].item()
+            self._sync_to_host()
             self._engine.close()
             self._engine = None
         self._globals_dirty = True

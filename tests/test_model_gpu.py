@@ -467,3 +467,28 @@ def test_breed_local_arrays_match_reference():
     m.reset()
     m.simulate(1)
     assert np.array_equal(m.get_breed_local_array("health"), d["health"][0])  # rebuilt from zeros
+
+
+def test_save_load_breed_ids_and_neighbor_visible(tmp_path):
+    """sagesim/model.py:1288-1309 (save / load), 492-515 (get_breed_agent_ids),
+    398-409 (set_property_neighbor_visible): a saved model continues from its
+    tick and state after loading, as the original does."""
+    want = chain_model(30, 0.5, 0.3, 5)
+    want.setup()
+    want.simulate(7)
+    m = chain_model(30, 0.5, 0.3, 5)
+    m.set_property_neighbor_visible("state", False)
+    with pytest.raises(ValueError):
+        m.set_property_neighbor_visible("no_such_property", True)
+    m.setup()
+    with pytest.raises(RuntimeError):
+        m.set_property_neighbor_visible("state", True)
+    assert m.get_breed_agent_ids("SIR").tolist() == list(range(30))
+    m.simulate(4)
+    path = str(tmp_path / "model.pkl")
+    m.save(m, path)
+    loaded = m.load(path)
+    assert loaded.tick == 4 and states(loaded, 30) == states(m, 30)
+    loaded.simulate(3)
+    m.simulate(3)
+    assert states(loaded, 30) == states(m, 30) == states(want, 30)
