@@ -272,8 +272,9 @@ class Model:
         gnames = [k for k, _ in sorted(self._global_names.items(), key=lambda kv: kv[1])]
         pdt = {k: ("i" if v[0] == np.int32 else "f") for k, v in self._props.items()}
         arrays = [(b["name"], b["shape_per_agent"]) for b in self._breed_local_arrays]
-        self._steps = [(pr, bi, (fn.translate(gnames, list(self._props), pdt, arrays) if isinstance(fn, PythonStep)
-                                 else fn), path) for pr, bi, fn, path in self._steps]
+        widths = {k: v[1] for k, v in self._props.items()}
+        self._steps = [(pr, bi, (fn.translate(gnames, list(self._props), pdt, arrays, widths)
+                                 if isinstance(fn, PythonStep) else fn), path) for pr, bi, fn, path in self._steps]
         self._pid = {}
         for name, (dt, width, arr) in self._props.items():
             self._pid[name] = e.add_property(name, dt, width, init=arr,

@@ -88,11 +88,11 @@ class PythonStep:
         self.source, self.name = find_step_source(step_func, module_fpath)
         self._writes = None
 
-    def translate(self, globals_, props, prop_dtypes, arrays=()):
+    def translate(self, globals_, props, prop_dtypes, arrays=(), prop_widths=None):
         from .translate import translate_step
 
         src, entry, writes = translate_step(self.source, self.name, globals_, props, prop_dtypes,
-                                            arrays=arrays)
+                                            arrays=arrays, prop_widths=prop_widths)
         self._writes = tuple(writes)
         return CudaStep(src, entry, writes=list(writes))
 

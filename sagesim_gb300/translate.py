@@ -24,7 +24,9 @@ comparisons, `and` / `or` / `not`; `int()`, `float()`, `bool()`, `abs()`, `min()
 `math` / `cp` `exp log sqrt sin cos tan tanh floor ceil fabs`;
 `rand_uniform_philox(tick, agent, salt)` and `rand_normal(tick, agent, salt)`;
 `locations[a]` (a neighbour row), `row[k]`, `len(row)`; property reads `p[a]`,
-`p[a][c]`, writes `p[a] = v`, `p[a][c] = v`; globals `g` and `g[k]`.
+`p[a][c]`, a local bound to a list property's row (`r = p[a]`, read as `r[c]`,
+`len(r)`; also `len(p[a])`), writes `p[a] = v`, `p[a][c] = v`; breed-local
+arrays `a[r][j]` (reads and writes) and their index maps; globals `g` and `g[k]`.
 
 Types follow numpy's scalar rules as CuPy-JIT does: Python int and float
 locals are int64 and float64, `cp.float32(...)` values are float32, a float32 with
@@ -101,7 +103,7 @@ def _promote(a, b):
 
 
 class _Translator:
-    def __init__(self, fn, globals_, props, prop_dtypes, entry, arrays=()):
+    def __init__(self, fn, globals_, props, prop_dtypes, entry, arrays=(), prop_widths=None):
         self.fn = fn
         self.entry = entry
         args = [a.arg for a in fn.args.args]
@@ -140,6 +142,8 @@ class _Translator:
         self.prop_dtypes = prop_dtypes
         self.locals = {}  # name -> type
         self.row_of = {}  # row local -> agent expression
+        self.widths = dict(prop_widths or {})  # list property -> values per agent
+        self.prow_of = {}  # local alias of a list property's row -> (property, agent expression)
         self.writes = set()
         self.out = []
 
@@ -167,6 +171,8 @@ class _Translator:
                 return "ctx.g[G_%s]" % self.globals[n.id], "d"
             if n.id in ("True", "False"):
                 return n.id.lower(), "b"
+            if n.id in self.prow_of:
+                self.err(n, "a property row is used only as row[k] or len(row)")
             if n.id in self.row_of:
                 return self.row_of[n.id], "row"
             if n.id in self.locals:
@@ -229,6 +235,11 @@ class _Translator:
                 return "floor((%s)(%s) / (%s)(%s))" % (_CT[t], a, _CT[t], b), t
             self.err(n, "float %% is not supported")
         if isinstance(op, ast.Pow):
+            e = n.right
+            if (t in ("i", "wi") and isinstance(e, ast.Constant) and isinstance(e.value, int)
+                    and not isinstance(e.value, bool) and 0 <= e.value <= 8):
+                # Python int ** small int literal: an exact integer product
+                return "(" + " * ".join(["(long long)(%s)" % a] * e.value or ["1LL"]) + ")", "i"
             return "pow((double)(%s), (double)(%s))" % (a, b), "d"
         sym = {ast.Add: "+", ast.Sub: "-", ast.Mult: "*", ast.BitAnd: "&", ast.BitOr: "|",
                ast.BitXor: "^", ast.LShift: "<<", ast.RShift: ">>"}.get(type(op))
@@ -294,6 +305,10 @@ class _Translator:
             if base.id in self.globals:
                 k, _ = self.expr(idx)
                 return "ctx.g[G_%s + (int)(%s)]" % (self.globals[base.id], k), "d"
+            if base.id in self.prow_of:
+                pname, a = self.prow_of[base.id]
+                c, _ = self.expr(idx)
+                return self.prop_read(n, pname, a, c)
             if base.id in self.row_of:
                 k, _ = self.expr(idx)
                 return "(long long)ctx.neighbor((int)(%s), (int)(%s))" % (self.row_of[base.id], k), "i"
@@ -319,10 +334,15 @@ class _Translator:
             return "ctx.%s((int)(%s), (long long)(%s))" % (m, a, s), "d"
         if name == "len" and mod is None:
             if len(args) == 1:
-                r, t = self.expr(args[0])
+                a0 = args[0]
+                if isinstance(a0, ast.Name) and a0.id in self.prow_of:
+                    return "(long long)ctx.width(PROP_%s)" % self.prow_of[a0.id][0], "i"
+                if self._list_prop_row(a0):
+                    return "(long long)ctx.width(PROP_%s)" % self.props[a0.value.id], "i"
+                r, t = self.expr(a0)
                 if t == "row":
                     return "(long long)ctx.degree((int)(%s))" % r, "i"
-            self.err(n, "len() of a neighbour row only")
+            self.err(n, "len() of a neighbour row or a list property's row only")
         if name == "isnan":
             a0 = args[0]
             if isinstance(a0, ast.Subscript) and self._is_row_element(a0):
@@ -365,6 +385,11 @@ class _Translator:
             return "%s((double)(%s))" % (name, s), "d"
         self.err(n, "unsupported call %s" % (ast.unparse(f) if hasattr(ast, "unparse") else name))
 
+    def _list_prop_row(self, n):
+        """Whether n is p[a] for a list property p (one agent's row)."""
+        return (isinstance(n, ast.Subscript) and isinstance(n.value, ast.Name) and n.value.id in self.props
+                and self.widths.get(self.props[n.value.id], 1) > 1 and not isinstance(n.slice, ast.Tuple))
+
     def _is_row_element(self, n):
         b = n.value
         if isinstance(b, ast.Name) and b.id in self.row_of:
@@ -394,6 +419,11 @@ class _Translator:
                     if isinstance(v, ast.Subscript) and isinstance(v.value, ast.Name) and v.value.id == self.locations:
                         self.locals[name] = "row"
                         self.row_of[name] = self.expr(v.slice)[0]
+                        continue
+                    if self._list_prop_row(v):
+                        # alias of one agent's row of a list property (read through row[k])
+                        self.locals[name] = "row"
+                        self.prow_of[name] = (self.props[v.value.id], self.expr(v.slice)[0])
                         continue
                     try:
                         _, t = self.expr(v)
@@ -490,6 +520,8 @@ class _Translator:
                 return self.emit("ctx.set_arr_f32(PROP_sgbla_%s, (long long)(%s), (float)(%s), %s);"
                                  % (aname, row, v, col), d)
             base, idx = tgt.value, tgt.slice
+            if isinstance(base, ast.Name) and base.id in self.prow_of:
+                self.err(node, "write a list property through the property (p[a][k] = v), not a row alias")
             comp = None
             if isinstance(base, ast.Subscript) and isinstance(base.value, ast.Name) and base.value.id in self.props:
                 pname = self.props[base.value.id]
@@ -529,7 +561,7 @@ def _load(t):
     return n
 
 
-def translate_step(source, name, globals_, props, prop_dtypes, entry=None, arrays=()):
+def translate_step(source, name, globals_, props, prop_dtypes, entry=None, arrays=(), prop_widths=None):
     """CUDA C++ for step `name` defined in `source`.
 
     globals_: the model's global property names in registration order.
@@ -538,7 +570,9 @@ def translate_step(source, name, globals_, props, prop_dtypes, entry=None, array
     (float32). arrays: the model's breed-local arrays in registration order as
     (name, shape per agent); each is read and written as the float32 engine
     array PROP_sgbla_<name> (row-major, one row per agent of its breed) with the
-    int32 index map PROP_sgbla_<name>_idx. Returns (C++ source, entry name,
+    int32 index map PROP_sgbla_<name>_idx. prop_widths: name -> values per
+    agent of list properties (a local bound to p[a] of such a property is an
+    alias of that row: row[k], len(row)). Returns (C++ source, entry name,
     properties and arrays written, the arrays as sgbla_<name>)."""
     tree = ast.parse(source)
     fn = None
@@ -549,5 +583,5 @@ def translate_step(source, name, globals_, props, prop_dtypes, entry=None, array
     if fn is None:
         raise StepTranslationError("no function %r in the step's source" % name)
     entry = entry or ("sg_py_" + name)
-    tr = _Translator(fn, list(globals_), list(props), dict(prop_dtypes), entry, arrays)
+    tr = _Translator(fn, list(globals_), list(props), dict(prop_dtypes), entry, arrays, prop_widths)
     return tr.run(), entry, sorted(tr.writes)

@@ -25,6 +25,9 @@ Outputs (committed; the tests read only these files):
                        breed-local arrays (one double-buffered, one written in
                        place at a later priority), both arrays after ticks
                        1, 2, 3, 5, 10, 25
+  measures_er.npz      1,500-agent ER graph, SIR with float32[4] protective
+                       measures and a float32[5] state-history ring (list
+                       properties read through row aliases), 25 ticks
   opinion_ws.npz       2,000-agent WS graph (k=10, p=0.1, seed 2), ordered
                        neighbours, float32 opinion + float32[8] weights, 50 ticks
 """
@@ -310,6 +313,50 @@ def bla_two_breeds():
                         load=np.stack(load))
 
 
+def measures_er():
+    from ref_steps import measures_step
+    from sagesim.breed import Breed
+    from sagesim.model import Model
+    from sagesim.space import NetworkSpace
+
+    from sagesim_gb300 import graphs
+
+    off, idx = graphs.erdos_renyi(1500, 0.004, 9)
+    n = off.size - 1
+    rng = np.random.default_rng(9)
+    st = np.ones(n, dtype=np.int32)
+    st[rng.choice(n, 30, replace=False)] = 2
+    meas = (rng.random((n, 4), dtype=np.float32) * np.float32(0.5)).astype(np.float32)
+    model = Model(NetworkSpace(), step_function_file_path="step_func_code_gold_meas.py")
+    br = Breed("SIR")
+    br.register_property("state", 1)
+    br.register_property("measures", [0.0] * 4)
+    br.register_property("history", [0.0] * 5)
+    br.register_step_func(measures_step, os.path.join(HERE, "ref_steps.py"), priority=0)
+    model.register_breed(br)
+    model.register_global_property("p_infection", 0.3)
+    model.register_global_property("p_recovery", 0.1)
+    model.set_seed(9)
+    for i in range(n):
+        model.create_agent_of_breed(br, state=int(st[i]), measures=[float(v) for v in meas[i]])
+    sp = model.get_space()
+    for i in range(n):
+        for k in range(off[i], off[i + 1]):
+            sp.connect_agents(i, int(idx[k]), directed=True)
+    model._max_blocks_per_sm = 1
+    model.setup(use_gpu=True)
+    keep = [1, 2, 5, 10, 25]
+    states, hist = [], []
+    for t in range(1, keep[-1] + 1):
+        model.simulate(1, sync_workers_every_n_ticks=1)
+        if t in keep:
+            states.append(states_by_agent(model, "state").astype(np.int8))
+            hist.append(states_by_agent(model, "history").astype(np.float32))
+    clear_generated()
+    np.savez_compressed(os.path.join(HERE, "measures_er.npz"), offsets=off, indices=idx, state0=st.astype(np.int8),
+                        measures=meas, ticks=np.array(keep), state=np.stack(states), history=np.stack(hist))
+
+
 def main():
     reference = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SAGESIM_REFERENCE", "")
     if not reference or not os.path.isdir(os.path.join(reference, "sagesim")):
@@ -317,9 +364,10 @@ def main():
     setup_paths(reference)
     work = tempfile.mkdtemp(prefix="sg_golden_")
     os.chdir(work)  # the reference writes its generated step module into the CWD
-    which = sys.argv[2:] or ["philox", "chain", "hier", "db", "er", "breeds", "bla", "opinion"]
+    which = sys.argv[2:] or ["philox", "chain", "hier", "db", "er", "breeds", "bla", "measures", "opinion"]
     jobs = {"philox": philox_vectors, "chain": chains, "hier": hierarchy, "db": db_priority,
-            "er": er_c1, "breeds": ba_breeds, "bla": bla_two_breeds, "opinion": opinion_ws}
+            "er": er_c1, "breeds": ba_breeds, "bla": bla_two_breeds, "measures": measures_er,
+            "opinion": opinion_ws}
     for w in which:
         print("generating", w, flush=True)
         jobs[w]()

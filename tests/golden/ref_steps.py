@@ -18,6 +18,12 @@ host_step / site_step: two breeds with breed-local arrays and no property
   Sites (priority 1) write load[row][tick % 2] = (neighbouring hosts' ticks
   infected, infected neighbouring hosts at tick start) in place
   (no_double_buffer) and add 0.5 to the other slot's count.
+measures_step: SIR with per-agent protective measures (a float32[4] list
+  property) and a float32[5] state-history ring, in the style of the SIR example
+  shipped with the reference but drawing philox(salt 1) instead of Python's
+  random(): a susceptible agent is infected when some neighbour is infected and
+  the draw is below p_infection * (1 - sum of pairwise products of the two
+  agents' measures / 16); rows are read through local aliases and len().
 opinion_step: weighted mean of the first min(deg, 8) ordered neighbours'
   opinions (float32 arithmetic in row order, normalised by the sum of |w|),
   plus noise_sigma * rand_normal(salt 1) in float64, clamped to [0, 1].
@@ -154,3 +160,31 @@ def site_step(
     load[row][slot][0] = tot
     load[row][slot][1] = cp.float32(k)
     load[row][1 - slot][1] += cp.float32(0.5)
+
+
+@jit.rawkernel(device="cuda")
+def measures_step(
+    tick, agent_index, p_infection, p_recovery,
+    agent_ids, breeds, locations, state_tensor, measures, history,
+):
+    neighbor_indices = locations[agent_index]
+    rand = rand_uniform_philox(tick, agent_index, 1)
+    agent_state = state_tensor[agent_index]
+    own = measures[agent_index]
+    if agent_state == 2 and rand < p_recovery:
+        state_tensor[agent_index] = 3
+    elif agent_state == 1:
+        i = 0
+        while i < len(neighbor_indices) and neighbor_indices[i] != -1:
+            nb = neighbor_indices[i]
+            theirs = measures[nb]
+            safety = 0.0
+            for a in range(len(own)):
+                for b in range(len(theirs)):
+                    safety += own[a] * theirs[b]
+            scaled = safety / (len(own) ** 2)
+            if state_tensor[nb] == 2 and rand < p_infection * (1 - scaled):
+                state_tensor[agent_index] = 2
+            i += 1
+    slot = tick % len(history[agent_index])
+    history[agent_index][slot] = state_tensor[agent_index]

@@ -492,3 +492,29 @@ def test_save_load_breed_ids_and_neighbor_visible(tmp_path):
     loaded.simulate(3)
     m.simulate(3)
     assert states(loaded, 30) == states(m, 30) == states(want, 30)
+
+
+def test_python_dialect_list_property_rows_match_reference():
+    """A reference-dialect step that reads list properties through row aliases
+    and len() (protective measures, a state-history ring), translated, against
+    the reference pipeline's states and histories (measures_er.npz)."""
+    d = gold("measures_er.npz")
+    off, idx = d["offsets"], d["indices"]
+    n = off.size - 1
+    m = Model(NetworkSpace())
+    br = Breed("SIR")
+    br.register_property("state", 1)
+    br.register_property("measures", [0.0] * 4)
+    br.register_property("history", [0.0] * 5)
+    br.register_step_func(_PyStepRef("measures_step"), REF_STEPS, 0)
+    m.register_breed(br)
+    m.register_global_property("p_infection", 0.3)
+    m.register_global_property("p_recovery", 0.1)
+    m.set_seed(9)
+    m.create_agents_bulk(br, n, state=d["state0"].astype(np.int32), measures=d["measures"])
+    m.get_space().set_csr(off, idx)
+    m.setup()
+    for j, t in enumerate(d["ticks"]):
+        m.simulate(int(t) - m.tick)
+        assert np.array_equal(m.get_property_array("state"), d["state"][j]), "state, tick %d" % t
+        assert np.array_equal(m.get_property_array("history"), d["history"][j]), "history, tick %d" % t

@@ -119,3 +119,24 @@ def step(tick, agent_index, p, agent_ids, breeds, locations, state, h, h_idx):
     bad = bad.replace("h[h_idx[agent_index]] = 1.0", "h_idx[agent_index] = 1")
     with pytest.raises(StepTranslationError):
         translate_step(bad, "step", ["p"], ["state"], {"state": "i"}, arrays=[("h", (3,))])
+
+
+def test_list_property_row_aliases():
+    """r = p[a] of a list property is an alias of that row: r[k] reads p[a][k],
+    len(r) and len(p[a]) are the property's width; writes through an alias are
+    refused; int ** small int literal stays an exact integer."""
+    src = open(os.path.join(GOLD, "ref_steps.py")).read()
+    code, _, writes = translate_step(src, "measures_step", ["p_infection", "p_recovery"],
+                                     ["state", "measures", "history"], {"state": "i", "measures": "f", "history": "f"},
+                                     prop_widths={"state": 1, "measures": 4, "history": 5})
+    assert writes == ["history", "state"]
+    assert "ctx.f32(PROP_measures, (int)(u_nb), (int)(u_b))" in code
+    assert "(long long)ctx.width(PROP_measures)" in code and "(long long)ctx.width(PROP_history)" in code
+    assert "pow(" not in code
+    bad = '''
+def step(tick, agent_index, p, agent_ids, breeds, locations, state, w):
+    r = w[agent_index]
+    r[0] = 1.0
+'''
+    with pytest.raises(StepTranslationError, match="row alias"):
+        translate_step(bad, "step", ["p"], ["state", "w"], {"state": "i", "w": "f"}, prop_widths={"w": 3})
