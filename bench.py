@@ -364,6 +364,8 @@ def serving_section(stream, device=0, n_requests=100, n_graphs=24):
             "served_agent_ticks_per_s": agent_ticks / out["wall_s"], "wall_s": out["wall_s"],
             "arrival_span_s": float(arrivals[-1]), "submit_s": out["submit_s"], "step_s": out["step_s"],
             "burst_agent_ticks_per_s": burst["agent_ticks"] / burst["wall_s"], "burst_wall_s": burst["wall_s"],
+            "burst_submit_s": burst["submit_s"], "burst_step_s": burst["step_s"],
+            "burst_step_agent_ticks_per_s": burst["agent_ticks"] / burst["step_s"],
             "burst_p50_latency_s": float(np.percentile(burst["latency_s"], 50)),
             "burst_p99_latency_s": float(np.percentile(burst["latency_s"], 99)),
             "plain_sequential_agent_ticks_per_s": agent_ticks / (plain_ms / 1e3),
