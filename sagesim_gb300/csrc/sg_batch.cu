@@ -115,6 +115,7 @@ void SgPool::destroy()
 {
     cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
+    copiers.reset();
     for (int h = 0; h < 2; ++h) {
         if (stage[h]) cudaFreeHost(stage[h]);
         if (stage_ev[h]) cudaEventDestroy(stage_ev[h]);
@@ -131,18 +132,6 @@ namespace {
 constexpr size_t kStageBytes = (size_t)32 << 20;
 constexpr size_t kStageMin = (size_t)4 << 20; // smaller uploads: one direct copy
 
-// dst[0, len) = src[0, len) with up to `threads` host threads.
-void parallel_copy(char *dst, const char *src, size_t len, unsigned threads)
-{
-    const size_t part = ((len + threads - 1) / threads + 63) & ~(size_t)63;
-    std::vector<std::thread> pool;
-    for (unsigned t = 1; t < threads && (size_t)t * part < len; ++t) {
-        const size_t b = (size_t)t * part, n = std::min(part, len - b);
-        pool.emplace_back([=] { memcpy(dst + b, src + b, n); });
-    }
-    memcpy(dst, src, std::min(part, len));
-    for (auto &th : pool) th.join();
-}
 } // namespace
 
 int SgPool::upload(void *dst, const void *src, size_t bytes)
@@ -157,12 +146,15 @@ int SgPool::upload(void *dst, const void *src, size_t bytes)
             POOL_CK(cudaEventCreateWithFlags(&stage_ev[h], cudaEventDisableTiming));
         }
     }
-    const unsigned threads = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+    if (!copiers) {
+        const unsigned hc = std::thread::hardware_concurrency();
+        copiers.reset(new SgCopyWorkers(hc > 1 ? std::min(7u, hc - 1) : 0u));
+    }
     int h = 0;
     for (size_t pos = 0; pos < bytes; pos += kStageBytes, h ^= 1) {
         const size_t len = std::min(kStageBytes, bytes - pos);
         POOL_CK(cudaEventSynchronize(stage_ev[h])); // this buffer's previous copy has left
-        parallel_copy((char *)stage[h], (const char *)src + pos, len, threads);
+        copiers->copy((char *)stage[h], (const char *)src + pos, len);
         POOL_CK(cudaMemcpyAsync((char *)dst + pos, stage[h], len, cudaMemcpyHostToDevice, stream));
         POOL_CK(cudaEventRecord(stage_ev[h], stream));
     }

@@ -13,8 +13,14 @@
 //   tiles        the work list of the kernels, tiles never straddle scenarios.
 // Space is handed out first-fit from free lists of agent and edge slots.
 #pragma once
+#include <algorithm>
+#include <condition_variable>
+#include <cstring>
 #include <map>
+#include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "sg_internal.h"
@@ -22,6 +28,87 @@
 // Agent slots of a scenario of n agents: n + 1, rounded up to a multiple of 32
 // (128-bit loads, and class-sweep mask words that belong to one scenario).
 inline int64_t sg_pool_agent_slots(int64_t n) { return (n + 1 + 31) & ~int64_t(31); }
+
+// Host threads that split a memcpy among themselves and the caller; started
+// once and kept (a thread start per copy costs more than the copy of a few MB).
+class SgCopyWorkers {
+  public:
+    explicit SgCopyWorkers(unsigned n)
+    {
+        for (unsigned i = 0; i < n; ++i) th_.emplace_back([this] { run(); });
+    }
+    ~SgCopyWorkers()
+    {
+        {
+            std::lock_guard<std::mutex> g(m_);
+            stop_ = true;
+        }
+        wake_.notify_all();
+        for (auto &t : th_) t.join();
+    }
+    SgCopyWorkers(const SgCopyWorkers &) = delete;
+    SgCopyWorkers &operator=(const SgCopyWorkers &) = delete;
+
+    // dst[0, len) = src[0, len); returns when every part is copied.
+    void copy(char *dst, const char *src, size_t len)
+    {
+        const unsigned parts = (unsigned)th_.size() + 1;
+        {
+            std::lock_guard<std::mutex> g(m_);
+            dst_ = dst;
+            src_ = src;
+            len_ = len;
+            part_ = ((len + parts - 1) / parts + 63) & ~(size_t)63;
+            parts_ = parts;
+            next_ = 0;
+            left_ = parts;
+            ++gen_;
+        }
+        wake_.notify_all();
+        work();
+        std::unique_lock<std::mutex> lk(m_);
+        done_.wait(lk, [this] { return left_ == 0; });
+    }
+
+  private:
+    void work()
+    {
+        for (;;) {
+            unsigned k;
+            {
+                std::lock_guard<std::mutex> g(m_);
+                if (next_ >= parts_) return;
+                k = next_++;
+            }
+            const size_t b = (size_t)k * part_;
+            if (b < len_) memcpy(dst_ + b, src_ + b, std::min(part_, len_ - b));
+            std::lock_guard<std::mutex> g(m_);
+            if (--left_ == 0) done_.notify_all();
+        }
+    }
+    void run()
+    {
+        unsigned long long seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> lk(m_);
+                wake_.wait(lk, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+            }
+            work();
+        }
+    }
+    std::vector<std::thread> th_;
+    std::mutex m_;
+    std::condition_variable wake_, done_;
+    char *dst_ = nullptr;
+    const char *src_ = nullptr;
+    size_t len_ = 0, part_ = 0;
+    unsigned parts_ = 0, next_ = 0, left_ = 0;
+    unsigned long long gen_ = 0;
+    bool stop_ = false;
+};
 
 struct SgPoolScen {
     int32_t sid = -1;
@@ -71,6 +158,7 @@ struct SgPool {
     // pageable memory runs far below the link's bandwidth.
     void *stage[2] = {nullptr, nullptr};
     cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+    std::unique_ptr<SgCopyWorkers> copiers; // started with the staging buffers
     int upload(void *dst, const void *src, size_t bytes);
     bool any_lids = false, all_symmetric = true;
     int64_t seg_cap = 0, tile_cap = 0, mega_cap = 0;
