@@ -160,7 +160,9 @@ int sg_last_error(const sg_engine *e, char *buf, size_t cap);
 /* CSR of the agent graph: agent i's neighbours are indices[offsets[i] ..
  * offsets[i+1]). Validates offsets[0] == 0, monotone offsets, offsets[n] == nnz
  * and every index in [0, n); SG_ERR_BAD_CSR otherwise. Replaces any previous
- * graph and fixes the agent count n. */
+ * graph and fixes the agent count n; once properties exist it may be called
+ * between runs with the same n (topology edits, sagesim/space.py:107-145): the
+ * next run rebuilds its tile tables and counts from the new graph. */
 int sg_set_graph_csr(sg_engine *e, const int32_t *offsets, int64_t n, const int32_t *indices,
                      int64_t nnz, int32_t flags);
 /* Graph from an edge list in agent ids, built on the GPU (replaces the
