@@ -224,3 +224,74 @@ def test_breed_local_array_registration():
     m._is_setup = True
     with pytest.raises(RuntimeError):
         m.register_breed_local_array("late", b, (1,))
+
+
+class _FakeEngine:
+    """Records the graph a Model hands to its engine (host-side test double)."""
+
+    def __init__(self):
+        self.graphs = []
+
+    def set_graph(self, off, idx, ordered=False):
+        self.graphs.append((np.array(off), np.array(idx), ordered))
+
+    def set_graph_from_ids(self, ids, src, dst, symmetric=True, ordered=False):
+        self.graphs.append(("ids", np.array(ids), np.array(src), np.array(dst), symmetric, ordered))
+
+
+def test_topology_edits_reach_the_engine_in_buffer_order():
+    """After setup, an edit of the space bumps its version and the next
+    simulate() hands the new CSR (buffer indices) to the engine; an unchanged
+    space hands nothing."""
+    m = Model(NetworkSpace())
+    b0, b1 = Breed("A"), Breed("B")
+    for b in (b0, b1):
+        b.register_property("state", 1)
+        m.register_breed(b)
+    for i in range(6):
+        m.create_agent_of_breed((b0, b1)[i % 2])
+    sp = m.get_space()
+    sp.connect_agents(0, 1)
+    m._collect_steps()
+    m._build_host_arrays()
+    m._engine = fake = _FakeEngine()
+    m._install_graph(fake)
+    m._refresh_graph()
+    assert len(fake.graphs) == 1
+    sp.connect_agents(2, 5)
+    sp.disconnect_agents(0, 1)
+    m._refresh_graph()
+    off, idx, _ = fake.graphs[-1]
+    pos = m._pos
+    rows = {a: set(idx[off[pos[a]]:off[pos[a] + 1]].tolist()) for a in range(6)}
+    assert rows[2] == {pos[5]} and rows[5] == {pos[2]} and rows[0] == set() and rows[1] == set()
+    sp.set_edges([0, 3], [4, 1], directed=True)
+    m._refresh_graph()
+    kind, ids, src, dst, sym, _ = fake.graphs[-1]
+    assert kind == "ids" and ids.tolist() == m._order.tolist() and not sym
+    assert src.tolist() == [0, 3] and dst.tolist() == [4, 1]
+    m._refresh_graph()  # nothing changed since: nothing handed over
+    assert len(fake.graphs) == 3
+
+
+def test_model_pickles_without_an_engine():
+    import pickle
+
+    m = Model(NetworkSpace(ordered=True))
+    b = Breed("SIR")
+    b.register_property("state", 1)
+    b.register_property("w", [0.0, 0.0])
+    b.register_step_func(STEP, __file__, 0)
+    m.register_breed(b)
+    m.register_global_property("p_infection", 0.5)
+    for i in range(4):
+        m.create_agent_of_breed(b, state=1 + (i == 2), w=[i, -i])
+    m.get_space().connect_agents(0, 3)
+    m.register_breed_local_array("h", b, (2,))
+    m._collect_steps()
+    m._build_host_arrays()
+    m2 = pickle.loads(pickle.dumps(m))
+    assert m2._engine is None and m2._order.tolist() == m._order.tolist()
+    assert m2.get_space().get_location(3) == [0]
+    assert m2.get_agent_property_value(2, "state") == 2 and m2.get_agent_property_value(1, "w") == [1, -1]
+    assert m2._breed_local_arrays[0]["shape_per_agent"] == (2,)
