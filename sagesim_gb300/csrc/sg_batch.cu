@@ -134,6 +134,15 @@ constexpr size_t kStageMin = (size_t)4 << 20; // smaller uploads: one direct cop
 
 } // namespace
 
+SgCopyWorkers &SgPool::workers()
+{
+    if (!copiers) {
+        const unsigned hc = std::thread::hardware_concurrency();
+        copiers.reset(new SgCopyWorkers(hc > 1 ? std::min(7u, hc - 1) : 0u));
+    }
+    return *copiers;
+}
+
 int SgPool::upload(void *dst, const void *src, size_t bytes)
 {
     if (bytes < kStageMin) {
@@ -146,15 +155,12 @@ int SgPool::upload(void *dst, const void *src, size_t bytes)
             POOL_CK(cudaEventCreateWithFlags(&stage_ev[h], cudaEventDisableTiming));
         }
     }
-    if (!copiers) {
-        const unsigned hc = std::thread::hardware_concurrency();
-        copiers.reset(new SgCopyWorkers(hc > 1 ? std::min(7u, hc - 1) : 0u));
-    }
+    SgCopyWorkers &cw = workers();
     int h = 0;
     for (size_t pos = 0; pos < bytes; pos += kStageBytes, h ^= 1) {
         const size_t len = std::min(kStageBytes, bytes - pos);
         POOL_CK(cudaEventSynchronize(stage_ev[h])); // this buffer's previous copy has left
-        copiers->copy((char *)stage[h], (const char *)src + pos, len);
+        cw.copy((char *)stage[h], (const char *)src + pos, len);
         POOL_CK(cudaMemcpyAsync((char *)dst + pos, stage[h], len, cudaMemcpyHostToDevice, stream));
         POOL_CK(cudaEventRecord(stage_ev[h], stream));
     }
@@ -284,10 +290,25 @@ int SgPool::place(const sg_scenario_desc &d, const int32_t *loff, const int32_t 
         for (int64_t i = 0; i < n; ++i) k[(size_t)i] = llids ? (uint32_t)(uint64_t)llids[i] : (uint32_t)i;
         POOL_CK(cudaMemcpyAsync(lids.as<uint32_t>() + ab, k.data(), (size_t)n * 4, cudaMemcpyHostToDevice, stream));
     }
-    // long rows (candidates for whole-block scans)
+    // long rows (candidates for whole-block scans), in index order; large
+    // scenarios scan their offsets on the worker threads
     std::vector<std::pair<int32_t, int32_t>> longs;
-    for (int64_t i = 0; i < n; ++i)
-        if (loff[i + 1] - loff[i] > kLongRowFloor) longs.push_back({(int32_t)i, loff[i + 1] - loff[i]});
+    auto scan_rows = [loff](int64_t b, int64_t e, std::vector<std::pair<int32_t, int32_t>> &out) {
+        for (int64_t i = b; i < e; ++i)
+            if (loff[i + 1] - loff[i] > kLongRowFloor) out.push_back({(int32_t)i, loff[i + 1] - loff[i]});
+    };
+    if (n < ((int64_t)1 << 20)) {
+        scan_rows(0, n, longs);
+    } else {
+        SgCopyWorkers &cw = workers();
+        const unsigned parts = cw.threads();
+        const int64_t step = (n + parts - 1) / parts;
+        std::vector<std::vector<std::pair<int32_t, int32_t>>> found(parts);
+        cw.run_parts(parts, [&](unsigned k) {
+            scan_rows(std::min(n, (int64_t)k * step), std::min(n, (int64_t)(k + 1) * step), found[k]);
+        });
+        for (auto &f : found) longs.insert(longs.end(), f.begin(), f.end());
+    }
     POOL_CK(cudaStreamSynchronize(stream)); // host staging vectors go out of scope
     s_long_rows_[sid] = std::move(longs);
     sid_slot[sid] = scen.size();

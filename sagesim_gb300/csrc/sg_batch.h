@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <condition_variable>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -29,8 +30,9 @@
 // (128-bit loads, and class-sweep mask words that belong to one scenario).
 inline int64_t sg_pool_agent_slots(int64_t n) { return (n + 1 + 31) & ~int64_t(31); }
 
-// Host threads that split a memcpy among themselves and the caller; started
-// once and kept (a thread start per copy costs more than the copy of a few MB).
+// Host threads that split a job (a memcpy, a scan) among themselves and the
+// caller; started once and kept (a thread start per piece of work costs more
+// than copying a few MB).
 class SgCopyWorkers {
   public:
     explicit SgCopyWorkers(unsigned n)
@@ -49,16 +51,15 @@ class SgCopyWorkers {
     SgCopyWorkers(const SgCopyWorkers &) = delete;
     SgCopyWorkers &operator=(const SgCopyWorkers &) = delete;
 
-    // dst[0, len) = src[0, len); returns when every part is copied.
-    void copy(char *dst, const char *src, size_t len)
+    unsigned threads() const { return (unsigned)th_.size() + 1; }
+
+    // Runs job(0) .. job(parts - 1) on the workers and the caller; returns when
+    // all have finished.
+    void run_parts(unsigned parts, std::function<void(unsigned)> job)
     {
-        const unsigned parts = (unsigned)th_.size() + 1;
         {
             std::lock_guard<std::mutex> g(m_);
-            dst_ = dst;
-            src_ = src;
-            len_ = len;
-            part_ = ((len + parts - 1) / parts + 63) & ~(size_t)63;
+            job_ = std::move(job);
             parts_ = parts;
             next_ = 0;
             left_ = parts;
@@ -68,6 +69,17 @@ class SgCopyWorkers {
         work();
         std::unique_lock<std::mutex> lk(m_);
         done_.wait(lk, [this] { return left_ == 0; });
+    }
+
+    // dst[0, len) = src[0, len), one part per thread.
+    void copy(char *dst, const char *src, size_t len)
+    {
+        const unsigned parts = threads();
+        const size_t part = ((len + parts - 1) / parts + 63) & ~(size_t)63;
+        run_parts(parts, [=](unsigned k) {
+            const size_t b = (size_t)k * part;
+            if (b < len) memcpy(dst + b, src + b, std::min(part, len - b));
+        });
     }
 
   private:
@@ -80,8 +92,7 @@ class SgCopyWorkers {
                 if (next_ >= parts_) return;
                 k = next_++;
             }
-            const size_t b = (size_t)k * part_;
-            if (b < len_) memcpy(dst_ + b, src_ + b, std::min(part_, len_ - b));
+            job_(k);
             std::lock_guard<std::mutex> g(m_);
             if (--left_ == 0) done_.notify_all();
         }
@@ -102,9 +113,7 @@ class SgCopyWorkers {
     std::vector<std::thread> th_;
     std::mutex m_;
     std::condition_variable wake_, done_;
-    char *dst_ = nullptr;
-    const char *src_ = nullptr;
-    size_t len_ = 0, part_ = 0;
+    std::function<void(unsigned)> job_;
     unsigned parts_ = 0, next_ = 0, left_ = 0;
     unsigned long long gen_ = 0;
     bool stop_ = false;
@@ -160,6 +169,7 @@ struct SgPool {
     cudaEvent_t stage_ev[2] = {nullptr, nullptr};
     std::unique_ptr<SgCopyWorkers> copiers; // started with the staging buffers
     int upload(void *dst, const void *src, size_t bytes);
+    SgCopyWorkers &workers(); // started on first use
     bool any_lids = false, all_symmetric = true;
     int64_t seg_cap = 0, tile_cap = 0, mega_cap = 0;
 
