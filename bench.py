@@ -46,6 +46,8 @@ SEED = 1
 MEASURED_TRAFFIC = {("count", 10_000_000, "sir_count_step"): 56.892e6}
 PARTS = 64
 CODES = (1, 2, 3)
+WORKLOAD = ("SIR per-infected-neighbour (salt 2+j trials), BA n=%d m=4 seed 1, 64-way locality relabel, "
+            "0.1%% infected, beta 0.03 gamma 0.07, 200 ticks")
 
 
 def _env_int(name, default):
@@ -452,9 +454,7 @@ def run_reference(args):
         "unit": "agent-ticks/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": N_AGENTS * TICKS / v * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": "SIR per-infected-neighbour, BA n=1e7 m=4 seed 1, 64-way relabel, "
-                               "0.1% infected, beta 0.03 gamma 0.07, 200 ticks",
-                   "sample": "%d ticks per step from tick 0" % sample},
+        "config": {"workload": WORKLOAD % N_AGENTS, "sample": "%d ticks per step from tick 0" % sample},
         "cpu_baseline": {"value": v, "unit": "agent-ticks/s", "cores": used, "kind": "port",
                          "sample": "%d ticks of the 200-tick run per step (C port of the reference "
                                    "tick, OpenMP)" % sample},
@@ -728,9 +728,7 @@ def main():
         "unit": "agent-ticks/s", "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
         "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": "SIR per-infected-neighbour (salt 2+j trials), BA n=%d m=4 seed 1, "
-                               "64-way locality relabel, 0.1%% infected, beta 0.03 gamma 0.07, 200 ticks"
-                               % n,
+        "config": {"workload": WORKLOAD % n,
                    "strategy": args.strategy, "nnz": nnz,
                    "l2": "inputs larger than L2 (CSR %.0f MB)" % (nnz * 4 / 1e6),
                    "parallelism": "replicas" if world > 1 else "single"},
