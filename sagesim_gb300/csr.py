@@ -4,6 +4,8 @@ Same results as sagesim/internal_utils.py:111-186 (build_csr_from_ragged,
 build_csr_values_only): offsets int32[n+1], values int32 in each row's own
 iteration order (set order for sets, insertion order for lists).
 """
+from itertools import chain
+
 import numpy as np
 
 
@@ -25,6 +27,9 @@ def build_csr_from_ragged(ragged_list):
 
 def build_csr_values_only(ragged_list, offsets):
     total = int(offsets[-1])
+    if all(isinstance(row, (set, list, tuple)) for row in ragged_list):
+        # every row a Python container: one pass over their concatenation
+        return np.fromiter(chain.from_iterable(ragged_list), dtype=np.int64, count=total).astype(np.int32)
     values = np.empty(total, dtype=np.int32)
     pos = 0
     for row in ragged_list:
