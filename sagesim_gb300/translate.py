@@ -23,6 +23,8 @@ comparisons, `and` / `or` / `not`; `int()`, `float()`, `bool()`, `abs()`, `min()
 `max()`, `len(row)`, `cp.float32()`, `cp.float64()`, `cp.int32()`, `cp.isnan()`,
 `math` / `cp` `exp log sqrt sin cos tan tanh floor ceil fabs`;
 `rand_uniform_philox(tick, agent, salt)` and `rand_normal(tick, agent, salt)`;
+the helpers of sagesim/utils.py (`get_num_neighbors`, `get_neighbor`,
+`get_this_agent_data_from_tensor`, `set_this_agent_data_from_tensor`);
 `locations[a]` (a neighbour row), `row[k]`, `len(row)`; property reads `p[a]`,
 `p[a][c]`, a local bound to a list property's row (`r = p[a]`, read as `r[c]`,
 `len(r)`; also `len(p[a])`), writes `p[a] = v`, `p[a][c] = v`; breed-local
@@ -323,6 +325,18 @@ class _Translator:
         name = f.id if isinstance(f, ast.Name) else (f.attr if isinstance(f, ast.Attribute) else None)
         mod = f.value.id if isinstance(f, ast.Attribute) and isinstance(f.value, ast.Name) else None
         args = n.args
+        # sagesim/utils.py device helpers
+        if name == "get_this_agent_data_from_tensor" and len(args) == 2:
+            sub = ast.Subscript(value=args[1], slice=args[0], ctx=ast.Load())
+            ast.copy_location(sub, n)
+            return self.subscript(sub)
+        if name == "get_num_neighbors" and len(args) == 2:
+            a, _ = self.expr(args[0])
+            return "(long long)ctx.degree((int)(%s))" % a, "i"
+        if name == "get_neighbor" and len(args) == 4:
+            a, _ = self.expr(args[0])
+            k, _ = self.expr(args[1])
+            return "(long long)ctx.neighbor((int)(%s), (int)(%s))" % (a, k), "i"
         if name in ("rand_uniform_philox", "rand_normal"):
             if len(args) != 3:
                 self.err(n, "%s takes (tick, agent, salt)" % name)
@@ -384,6 +398,11 @@ class _Translator:
                 return "%sf(%s)" % (name, s), "f"
             return "%s((double)(%s))" % (name, s), "d"
         self.err(n, "unsupported call %s" % (ast.unparse(f) if hasattr(ast, "unparse") else name))
+
+    @staticmethod
+    def _helper_name(call):
+        f = call.func
+        return f.id if isinstance(f, ast.Name) else (f.attr if isinstance(f, ast.Attribute) else None)
 
     def _list_prop_row(self, n):
         """Whether n is p[a] for a list property p (one agent's row)."""
@@ -452,6 +471,13 @@ class _Translator:
         if isinstance(s, ast.Expr):
             if isinstance(s.value, ast.Constant) and isinstance(s.value.value, str):
                 return  # docstring
+            v = s.value
+            if (isinstance(v, ast.Call) and self._helper_name(v) == "set_this_agent_data_from_tensor"
+                    and len(v.args) == 3):
+                # sagesim/utils.py: set_this_agent_data_from_tensor(a, p, x) is p[a] = x
+                tgt = ast.Subscript(value=v.args[1], slice=v.args[0], ctx=ast.Store())
+                ast.copy_location(tgt, s)
+                return self.assign(tgt, v.args[2], d, s)
             self.err(s, "expression statements are not supported")
         if isinstance(s, ast.Pass):
             return

@@ -28,6 +28,8 @@ Outputs (committed; the tests read only these files):
   measures_er.npz      1,500-agent ER graph, SIR with float32[4] protective
                        measures and a float32[5] state-history ring (list
                        properties read through row aliases), 25 ticks
+  helpers_er.npz       1,000-agent ER graph, per-neighbour SIR written with the
+                       device helpers of sagesim/utils.py, 30 ticks
   opinion_ws.npz       2,000-agent WS graph (k=10, p=0.1, seed 2), ordered
                        neighbours, float32 opinion + float32[8] weights, 50 ticks
 """
@@ -357,6 +359,41 @@ def measures_er():
                         measures=meas, ticks=np.array(keep), state=np.stack(states), history=np.stack(hist))
 
 
+def helpers_er():
+    from ref_steps import helpers_step
+    from sagesim.breed import Breed
+    from sagesim.model import Model
+    from sagesim.space import NetworkSpace
+
+    from sagesim_gb300 import graphs
+
+    off, idx = graphs.erdos_renyi(1000, 0.006, 12)
+    n = off.size - 1
+    rng = np.random.default_rng(12)
+    st = np.ones(n, dtype=np.int32)
+    st[rng.choice(n, 15, replace=False)] = 2
+    model = Model(NetworkSpace(), step_function_file_path="step_func_code_gold_helpers.py")
+    br = Breed("SIR")
+    br.register_property("state", 1)
+    br.register_property("visits", 0.0)
+    br.register_step_func(helpers_step, os.path.join(HERE, "ref_steps.py"), priority=0)
+    model.register_breed(br)
+    model.register_global_property("p_infection", 0.2)
+    model.register_global_property("p_recovery", 0.1)
+    model.set_seed(12)
+    for i in range(n):
+        model.create_agent_of_breed(br, state=int(st[i]))
+    sp = model.get_space()
+    for i in range(n):
+        for k in range(off[i], off[i + 1]):
+            sp.connect_agents(i, int(idx[k]), directed=True)
+    hist = run_ticks(model, "state", 30, np.int8)
+    visits = states_by_agent(model, "visits").astype(np.float32)
+    clear_generated()
+    np.savez_compressed(os.path.join(HERE, "helpers_er.npz"), offsets=off, indices=idx, state0=st.astype(np.int8),
+                        history=hist, visits=visits)
+
+
 def main():
     reference = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SAGESIM_REFERENCE", "")
     if not reference or not os.path.isdir(os.path.join(reference, "sagesim")):
@@ -364,9 +401,10 @@ def main():
     setup_paths(reference)
     work = tempfile.mkdtemp(prefix="sg_golden_")
     os.chdir(work)  # the reference writes its generated step module into the CWD
-    which = sys.argv[2:] or ["philox", "chain", "hier", "db", "er", "breeds", "bla", "measures", "opinion"]
+    which = sys.argv[2:] or ["philox", "chain", "hier", "db", "er", "breeds", "bla", "measures", "helpers",
+                             "opinion"]
     jobs = {"philox": philox_vectors, "chain": chains, "hier": hierarchy, "db": db_priority,
-            "er": er_c1, "breeds": ba_breeds, "bla": bla_two_breeds, "measures": measures_er,
+            "er": er_c1, "breeds": ba_breeds, "bla": bla_two_breeds, "measures": measures_er, "helpers": helpers_er,
             "opinion": opinion_ws}
     for w in which:
         print("generating", w, flush=True)

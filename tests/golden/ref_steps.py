@@ -24,6 +24,9 @@ measures_step: SIR with per-agent protective measures (a float32[4] list
   random(): a susceptible agent is infected when some neighbour is infected and
   the draw is below p_infection * (1 - sum of pairwise products of the two
   agents' measures / 16); rows are read through local aliases and len().
+helpers_step: per-neighbour SIR written with the device helpers of
+  sagesim/utils.py (get_num_neighbors / get_neighbor on the CSR names,
+  get_ / set_this_agent_data_from_tensor) plus a float32 visit counter.
 opinion_step: weighted mean of the first min(deg, 8) ordered neighbours'
   opinions (float32 arithmetic in row order, normalised by the sum of |w|),
   plus noise_sigma * rand_normal(salt 1) in float64, clamped to [0, 1].
@@ -32,6 +35,12 @@ import cupy as cp
 from cupyx import jit
 
 from sagesim.math_utils import rand_normal, rand_uniform_philox
+from sagesim.utils import (
+    get_neighbor,
+    get_num_neighbors,
+    get_this_agent_data_from_tensor,
+    set_this_agent_data_from_tensor,
+)
 
 
 @jit.rawkernel(device="cuda")
@@ -188,3 +197,27 @@ def measures_step(
             i += 1
     slot = tick % len(history[agent_index])
     history[agent_index][slot] = state_tensor[agent_index]
+
+
+@jit.rawkernel(device="cuda")
+def helpers_step(
+    tick, agent_index, p_infection, p_recovery,
+    agent_ids, breeds, locations, state_tensor, visits,
+):
+    agent_state = int(get_this_agent_data_from_tensor(agent_index, state_tensor))
+    if agent_state == 2:
+        if rand_uniform_philox(tick, agent_index, 1) < p_recovery:
+            set_this_agent_data_from_tensor(agent_index, state_tensor, 3)
+    elif agent_state == 1:
+        i = 0
+        j = 0
+        infected = False
+        while i < get_num_neighbors(agent_index, neighbor_offsets) and not infected:
+            nb = get_neighbor(agent_index, i, neighbor_offsets, neighbor_values)
+            if int(state_tensor[nb]) == 2:
+                if rand_uniform_philox(tick, agent_index, 2 + j) < p_infection:
+                    set_this_agent_data_from_tensor(agent_index, state_tensor, 2)
+                    infected = True
+                j += 1
+            i += 1
+    visits[agent_index] = visits[agent_index] + 1

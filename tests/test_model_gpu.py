@@ -518,3 +518,29 @@ def test_python_dialect_list_property_rows_match_reference():
         m.simulate(int(t) - m.tick)
         assert np.array_equal(m.get_property_array("state"), d["state"][j]), "state, tick %d" % t
         assert np.array_equal(m.get_property_array("history"), d["history"][j]), "history, tick %d" % t
+
+
+def test_python_dialect_utils_helpers_match_reference():
+    """A reference-dialect step written with sagesim/utils.py's device helpers
+    (get_num_neighbors / get_neighbor on the CSR names, get_ / set_this_agent_
+    data_from_tensor), translated, against the reference pipeline's every-tick
+    states and final visit counters (helpers_er.npz)."""
+    d = gold("helpers_er.npz")
+    off, idx = d["offsets"], d["indices"]
+    n = off.size - 1
+    m = Model(NetworkSpace())
+    br = Breed("SIR")
+    br.register_property("state", 1)
+    br.register_property("visits", 0.0)
+    br.register_step_func(_PyStepRef("helpers_step"), REF_STEPS, 0)
+    m.register_breed(br)
+    m.register_global_property("p_infection", 0.2)
+    m.register_global_property("p_recovery", 0.1)
+    m.set_seed(12)
+    m.create_agents_bulk(br, n, state=d["state0"].astype(np.int32))
+    m.get_space().set_csr(off, idx)
+    m.setup()
+    for t in range(30):
+        m.simulate(1)
+        assert np.array_equal(m.get_property_array("state"), d["history"][t]), "tick %d" % t
+    assert np.array_equal(m.get_property_array("visits"), d["visits"])

@@ -140,3 +140,15 @@ def step(tick, agent_index, p, agent_ids, breeds, locations, state, w):
 '''
     with pytest.raises(StepTranslationError, match="row alias"):
         translate_step(bad, "step", ["p"], ["state", "w"], {"state": "i", "w": "f"}, prop_widths={"w": 3})
+
+
+def test_utils_helpers():
+    """sagesim/utils.py's device helpers: get_num_neighbors / get_neighbor read
+    the CSR, get_ / set_this_agent_data_from_tensor are p[a] and p[a] = x."""
+    src = open(os.path.join(GOLD, "ref_steps.py")).read()
+    code, _, writes = translate_step(src, "helpers_step", ["p_infection", "p_recovery"], ["state", "visits"],
+                                     {"state": "i", "visits": "f"})
+    assert writes == ["state", "visits"]
+    assert "ctx.degree((int)(sg_agent))" in code and "ctx.neighbor((int)(sg_agent), (int)(u_i))" in code
+    assert "ctx.set_i32(PROP_state, (int)(sg_agent), (int)(3LL));" in code
+    assert "ctx.i32(PROP_state, (int)(sg_agent))" in code
