@@ -154,6 +154,24 @@ def ensemble_specs(count=512, seed=3):
     return specs, params
 
 
+def max_over_ranks(value, dist=None, device=None):
+    """The largest of every rank's value: a job of replicas ends with its slowest
+    one (identity on a single process)."""
+    if dist is None:
+        return float(value)
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(units_per_rank, world, seconds):
+    """Whole-job rate of `world` independent replicas that each process
+    units_per_rank units, the slowest in `seconds`."""
+    return world * units_per_rank / seconds
+
+
 def initial_state(n, frac, seed):
     st = np.full(n, CODES[0], dtype=np.int32)
     k = max(1, int(round(frac * n)))
@@ -639,11 +657,7 @@ def main():
             ev1.record(stream)
             stream.synchronize()
             clocks = clk.stop()
-            ms = ev0.elapsed_time(ev1)
-            if dist:
-                t = torch.tensor([ms], device="cuda")
-                dist.all_reduce(t, op=dist.ReduceOp.MAX)
-                ms = float(t.item())
+            ms = max_over_ranks(ev0.elapsed_time(ev1), dist, "cuda")
             ms_step = ms / steps
 
             # end to end through the C ABI with pinned host buffers
@@ -658,7 +672,7 @@ def main():
                 eng.set_property_ptr(prop, h_in.data_ptr(), 0, n)
                 eng.run_async(0, TICKS, use_graph=True)
                 eng.get_property_ptr(prop, h_out.data_ptr(), 0, n)
-            e2e_s = (time.perf_counter() - t0) / steps
+            e2e_s = max_over_ranks((time.perf_counter() - t0) / steps, dist, "cuda")
             if not np.array_equal(h_out.numpy(), final):
                 raise RuntimeError("end-to-end result differs from the device-resident run")
 
@@ -683,8 +697,9 @@ def main():
         own_achieved = own / (per_launch_ms / 1e3) / 1e9
         traffic = MEASURED_TRAFFIC.get((strategy, n, dom_name))
         return {
-            "value": world * n * TICKS / (ms_step / 1e3), "ms_per_step": ms_step,
-            "e2e": world * n * TICKS / e2e_s, "edge_visits_per_s": world * float(E_S.sum()) / (ms_step / 1e3),
+            "value": replica_rate(n * TICKS, world, ms_step / 1e3), "ms_per_step": ms_step,
+            "e2e": replica_rate(n * TICKS, world, e2e_s),
+            "edge_visits_per_s": replica_rate(float(E_S.sum()), world, ms_step / 1e3),
             "launches": steps * run_launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "kernel": dom_name,
