@@ -66,6 +66,18 @@ __device__ __forceinline__ long long sg_py_mod(long long a, long long b)
     if (m != 0 && ((m < 0) != (b < 0))) m += b;
     return m;
 }
+__device__ __forceinline__ double sg_py_fmod(double a, double b)
+{
+    double m = fmod(a, b);
+    if (m != 0.0 && ((m < 0.0) != (b < 0.0))) m += b;
+    return m;
+}
+__device__ __forceinline__ float sg_py_fmodf(float a, float b)
+{
+    float m = fmodf(a, b);
+    if (m != 0.0f && ((m < 0.0f) != (b < 0.0f))) m += b;
+    return m;
+}
 """
 
 
@@ -235,7 +247,10 @@ class _Translator:
             if isinstance(op, ast.FloorDiv):
                 t = "d" if t == "wf" else t
                 return "floor((%s)(%s) / (%s)(%s))" % (_CT[t], a, _CT[t], b), t
-            self.err(n, "float %% is not supported")
+            # Python / numpy float remainder: the sign of the divisor
+            t = "d" if t == "wf" else t
+            f = "sg_py_fmodf" if t == "f" else "sg_py_fmod"
+            return "%s((%s)(%s), (%s)(%s))" % (f, _CT[t], a, _CT[t], b), t
         if isinstance(op, ast.Pow):
             e = n.right
             if (t in ("i", "wi") and isinstance(e, ast.Constant) and isinstance(e.value, int)

@@ -152,3 +152,17 @@ def test_utils_helpers():
     assert "ctx.degree((int)(sg_agent))" in code and "ctx.neighbor((int)(sg_agent), (int)(u_i))" in code
     assert "ctx.set_i32(PROP_state, (int)(sg_agent), (int)(3LL));" in code
     assert "ctx.i32(PROP_state, (int)(sg_agent))" in code
+
+
+def test_float_remainder_has_python_sign():
+    """x % y on floats follows Python / numpy (the result takes the divisor's
+    sign): fmod, then the divisor added when the signs differ."""
+    src = '''
+def step(tick, agent_index, p, agent_ids, breeds, locations, x):
+    a = 5.5 % 2.0
+    b = x[agent_index] % cp.float32(0.25)
+'''
+    code, _, _ = translate_step(src, "step", ["p"], ["x"], {"x": "f"})
+    assert "double u_a" in code and "u_a = (double)(sg_py_fmod((double)(5.5), (double)(2.0)));" in code
+    assert "float u_b" in code and "sg_py_fmodf((float)(ctx.f32(PROP_x, (int)(sg_agent)))" in code
+    assert "if (m != 0.0 && ((m < 0.0) != (b < 0.0))) m += b;" in code
