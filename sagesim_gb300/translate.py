@@ -33,7 +33,8 @@ arrays `a[r][j]` (reads and writes) and their index maps; globals `g` and `g[k]`
 Types follow numpy's scalar rules as CuPy-JIT does: Python int and float
 locals are int64 and float64, `cp.float32(...)` values are float32, a float32 with
 an int64 or float64 operand becomes float64, Python number literals take the other
-operand's type, `/` is true division. Integer `//` and `%` keep Python's flooring
+operand's type, `/` is true division, float `%` takes the divisor's sign (the
+helpers for it are emitted only into steps that use it). Integer `//` and `%` keep Python's flooring
 semantics. Anything outside the subset raises `StepTranslationError` naming the
 line.
 """
@@ -66,6 +67,9 @@ __device__ __forceinline__ long long sg_py_mod(long long a, long long b)
     if (m != 0 && ((m < 0) != (b < 0))) m += b;
     return m;
 }
+"""
+# emitted only for steps that take a float remainder
+_PRELUDE_FMOD = r"""
 __device__ __forceinline__ double sg_py_fmod(double a, double b)
 {
     double m = fmod(a, b);
@@ -159,6 +163,7 @@ class _Translator:
         self.widths = dict(prop_widths or {})  # list property -> values per agent
         self.prow_of = {}  # local alias of a list property's row -> (property, agent expression)
         self.writes = set()
+        self.need_fmod = False
         self.out = []
 
     def err(self, node, msg):
@@ -249,6 +254,7 @@ class _Translator:
                 return "floor((%s)(%s) / (%s)(%s))" % (_CT[t], a, _CT[t], b), t
             # Python / numpy float remainder: the sign of the divisor
             t = "d" if t == "wf" else t
+            self.need_fmod = True
             f = "sg_py_fmodf" if t == "f" else "sg_py_fmod"
             return "%s((%s)(%s), (%s)(%s))" % (f, _CT[t], a, _CT[t], b), t
         if isinstance(op, ast.Pow):
@@ -590,7 +596,8 @@ class _Translator:
         self.scan(self.fn.body)
         decls = ["    %s u_%s = 0;" % (_CT[t], name) for name, t in self.locals.items() if t != "row"]
         self.block(self.fn.body, 1)
-        src = [_PRELUDE, "__device__ void %s(const sg_ctx &ctx, int sg_agent)" % self.entry, "{"]
+        prelude = _PRELUDE + (_PRELUDE_FMOD if self.need_fmod else "")
+        src = [prelude, "__device__ void %s(const sg_ctx &ctx, int sg_agent)" % self.entry, "{"]
         src += decls
         src += self.out
         src.append("}")
