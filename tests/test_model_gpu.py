@@ -544,3 +544,27 @@ def test_python_dialect_utils_helpers_match_reference():
         m.simulate(1)
         assert np.array_equal(m.get_property_array("state"), d["history"][t]), "tick %d" % t
     assert np.array_equal(m.get_property_array("visits"), d["visits"])
+
+
+def test_python_dialect_float_remainder(tmp_path):
+    """Float % in a translated step has Python's sign rule (numpy.remainder)."""
+    mod = tmp_path / "fmod_step.py"
+    mod.write_text('''
+def fmod_step(tick, agent_index, d, agent_ids, breeds, locations, x, y):
+    y[agent_index] = x[agent_index] % d
+''')
+    n = 64
+    x = np.linspace(-7.3, 7.3, n).astype(np.float32)
+    m = Model(NetworkSpace())
+    br = Breed("B")
+    br.register_property("x", 0.5)
+    br.register_property("y", 0.5)
+    br.register_step_func(_PyStepRef("fmod_step"), str(mod), 0)
+    m.register_breed(br)
+    m.register_global_property("d", -2.5)
+    m.create_agents_bulk(br, n, x=x)
+    m.get_space().set_csr(np.zeros(n + 1, dtype=np.int32), np.zeros(0, dtype=np.int32))
+    m.setup()
+    m.simulate(1)
+    want = np.remainder(x.astype(np.float64), -2.5).astype(np.float32)
+    assert np.array_equal(m.get_property_array("y"), want)
