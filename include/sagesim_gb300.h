@@ -226,6 +226,11 @@ int sg_compile_step(sg_engine *e, const char *cuda_src, const char *entry, int32
  * tick_stats (nullable, host): 4 int64 per tick = S, I, R after the tick and E_S,
  * summed over the SIR steps. out (nullable) gets totals. Synchronous. */
 int sg_run(sg_engine *e, int64_t tick0, int32_t nticks, int64_t *tick_stats, sg_stats *out);
+/* Per-tick history for parity dumps: the S, I, R, E_S rows (as in tick_stats)
+ * of consecutive sg_run calls that took statistics, from the tick *first_tick
+ * on; a run that does not continue them starts a new history. Copies up to
+ * max_ticks rows into out (nullable) and returns the row count in *nticks. */
+int sg_get_tick_history(sg_engine *e, int64_t *out, int64_t max_ticks, int64_t *nticks, int64_t *first_tick);
 /* Same, asynchronous on the engine stream: returns after enqueueing (through a
  * CUDA graph of the tick loop when use_graph != 0). No stats. */
 int sg_run_async(sg_engine *e, int64_t tick0, int32_t nticks, int32_t use_graph);

@@ -116,6 +116,7 @@ SIGNATURES = {
     "sg_set_globals_f64": [_P, _P, _I32],
     "sg_add_property": [_P, _C, _I32, _I32, _I32, _P, ctypes.POINTER(_I32)],
     "sg_add_array": [_P, _C, _I32, _I32, _I64, _I32, _P, ctypes.POINTER(_I32)],
+    "sg_get_tick_history": [_P, _P, _I64, ctypes.POINTER(_I64), ctypes.POINTER(_I64)],
     "sg_set_property": [_P, _I32, _P, _I64, _I64],
     "sg_get_property": [_P, _I32, _P, _I64, _I64],
     "sg_property_device_ptr": [_P, _I32, ctypes.POINTER(_P)],

@@ -95,6 +95,8 @@ struct sg_engine {
                  SG_FLAVOUR_SWEEP | SG_FLAVOUR_HYBRID | SG_FLAVOUR_DENSE | SG_FLAVOUR_LAZY, 0.0};
     int32_t last_nticks = 0;
     int64_t last_launches = 0; // kernels launched by the last enqueued run
+    std::vector<int64_t> hist;  // per-tick S, I, R, E_S of consecutive runs with statistics
+    int64_t hist_tick0 = 0;     // tick of hist's first row
 
     // CUDA graph of the tick loop (sg_run_async with use_graph)
     cudaGraphExec_t graph_exec = nullptr;
@@ -985,6 +987,12 @@ int sg_run(sg_engine *e, int64_t tick0, int32_t nticks, int64_t *tick_stats, sg_
         }
         if (tick_stats)
             for (size_t k = 0; k < st.size(); ++k) tick_stats[k] = (int64_t)st[k];
+        // a run that does not continue the recorded ticks starts a new history
+        if (tick0 != e->hist_tick0 + (int64_t)(e->hist.size() / 4)) {
+            e->hist.clear();
+            e->hist_tick0 = tick0;
+        }
+        for (unsigned long long v : st) e->hist.push_back((int64_t)v);
     }
     if (out) {
         out->ticks = nticks;
@@ -998,6 +1006,17 @@ int sg_run(sg_engine *e, int64_t tick0, int32_t nticks, int64_t *tick_stats, sg_
         out->device_ms = ms;
         out->kernel_launches = e->last_launches;
     }
+    return SG_OK;
+}
+
+int sg_get_tick_history(sg_engine *e, int64_t *out, int64_t max_ticks, int64_t *nticks, int64_t *first_tick)
+{
+    if (!e || max_ticks < 0) return SG_ERR_INVALID;
+    const int64_t rows = (int64_t)(e->hist.size() / 4);
+    if (nticks) *nticks = rows;
+    if (first_tick) *first_tick = e->hist_tick0;
+    const int64_t k = std::min(rows, max_ticks);
+    if (out && k > 0) memcpy(out, e->hist.data(), (size_t)k * 4 * sizeof(int64_t));
     return SG_OK;
 }
 

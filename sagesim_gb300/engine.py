@@ -215,6 +215,17 @@ class Engine:
     def synchronize(self):
         self._ck(self._lib.sg_synchronize(self._h))
 
+    def tick_history(self):
+        """(first tick, int64[ticks, 4] of S, I, R, E_S) recorded by consecutive
+        run() calls with statistics."""
+        rows, first = ctypes.c_int64(), ctypes.c_int64()
+        self._ck(self._lib.sg_get_tick_history(self._h, None, 0, ctypes.byref(rows), ctypes.byref(first)))
+        out = np.zeros((rows.value, 4), dtype=np.int64)
+        if rows.value:
+            self._ck(self._lib.sg_get_tick_history(self._h, _ptr(out), rows.value, ctypes.byref(rows),
+                                                   ctypes.byref(first)))
+        return first.value, out
+
     def snapshot(self):
         self._ck(self._lib.sg_snapshot(self._h))
 

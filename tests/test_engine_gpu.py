@@ -197,3 +197,24 @@ __device__ void f(const sg_ctx &ctx, int i)
         a2 = e.add_array("a2", np.int32, 1, rows)
         with pytest.raises(SageSimError, match="agent property"):
             e.add_sir(a2, 0.1, 0.1)  # an array is not an agent property
+
+
+def test_tick_history_across_runs():
+    """sg_get_tick_history: consecutive runs add their per-tick S, I, R, E_S rows;
+    a run from another tick starts a new history."""
+    off, idx = graphs.erdos_renyi(5000, 0.002, 4)
+    st0 = np.ones(5000, dtype=np.int32)
+    st0[:50] = 2
+    with Engine() as e:
+        e.set_graph(off, idx, symmetric=True)
+        p = e.add_property("state", np.int32, init=st0)
+        e.add_sir(p, 0.1, 0.1, variant="B")
+        e.snapshot()
+        a, _ = e.run(0, 10)
+        b, _ = e.run(10, 5)
+        first, hist = e.tick_history()
+        assert first == 0 and np.array_equal(hist, np.vstack([a, b]))
+        e.restore()
+        c, _ = e.run(0, 3)
+        first, hist = e.tick_history()
+        assert first == 0 and np.array_equal(hist, c) and np.array_equal(c, a[:3])
