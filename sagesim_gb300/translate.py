@@ -20,7 +20,7 @@ Supported subset (what the reference's own step functions use): assignments and
 augmented assignments to locals and to property elements, `if` / `elif` / `else`,
 `while`, `for ... in range(...)`, `break`, `continue`, bare `return`; arithmetic,
 comparisons, `and` / `or` / `not`; `int()`, `float()`, `bool()`, `abs()`, `min()`,
-`max()`, `len(row)`, `cp.float32()`, `cp.float64()`, `cp.int32()`, `cp.isnan()`,
+`max()` (of two or more values), `math` / `cp` `pi` and `e`, `len(row)`, `cp.float32()`, `cp.float64()`, `cp.int32()`, `cp.isnan()`,
 `math` / `cp` `exp log sqrt sin cos tan tanh floor ceil fabs`;
 `rand_uniform_philox(tick, agent, salt)` and `rand_normal(tick, agent, salt)`;
 the helpers of sagesim/utils.py (`get_num_neighbors`, `get_neighbor`,
@@ -53,6 +53,7 @@ class StepTranslationError(ValueError):
 # types: "i" int64, "f" float32, "d" float64, "b" bool, "row" neighbour row,
 # "wi" / "wf" weak (literal) int / float
 _CT = {"i": "long long", "f": "float", "d": "double", "b": "bool"}
+_CONSTS = {"pi": "3.141592653589793", "e": "2.718281828459045"}
 _MATH = {"exp", "log", "sqrt", "sin", "cos", "tan", "tanh", "floor", "ceil", "fabs", "log10", "log2"}
 _PRELUDE = r"""
 __device__ __forceinline__ long long sg_py_floordiv(long long a, long long b)
@@ -230,6 +231,9 @@ class _Translator:
             t = _promote(at, bt)
             t = "i" if t == "wi" else ("d" if t == "wf" else t)
             return "((%s) ? (%s)(%s) : (%s)(%s))" % (c, _CT[t], a, _CT[t], b), t
+        if isinstance(n, ast.Attribute) and isinstance(n.value, ast.Name) and \
+                n.value.id in ("math", "cp", "np", "numpy", "cupy") and n.attr in _CONSTS:
+            return _CONSTS[n.attr], "wf"  # a Python float: weak in numpy's promotion
         if isinstance(n, ast.Subscript):
             return self.subscript(n)
         if isinstance(n, ast.Call):
@@ -404,15 +408,17 @@ class _Translator:
                 return "llabs((long long)(%s))" % s, "i"
             return "fabs((double)(%s))" % s, "d"
         if name in ("min", "max") and mod is None:
-            if len(args) != 2:
-                self.err(n, "min/max of two values only")
+            if len(args) < 2:
+                self.err(n, "min/max of two or more values only")
             a, at = self.expr(args[0])
-            b, bt = self.expr(args[1])
-            t = _promote(at, bt)
-            t = "i" if t == "wi" else ("d" if t == "wf" else t)
             op = "<" if name == "min" else ">"
-            return "((%s)(%s) %s (%s)(%s) ? (%s)(%s) : (%s)(%s))" % (
-                _CT[t], a, op, _CT[t], b, _CT[t], a, _CT[t], b), t
+            for arg in args[1:]:  # left to right, as Python folds them
+                b, bt = self.expr(arg)
+                t = _promote(at, bt)
+                t = "i" if t == "wi" else ("d" if t == "wf" else t)
+                a, at = "((%s)(%s) %s (%s)(%s) ? (%s)(%s) : (%s)(%s))" % (
+                    _CT[t], a, op, _CT[t], b, _CT[t], a, _CT[t], b), t
+            return a, at
         if name in _MATH and mod in ("math", "cp", "np", "numpy", "cupy"):
             s, t = self.expr(args[0])
             if t == "f" and mod != "math":

@@ -166,3 +166,20 @@ def step(tick, agent_index, p, agent_ids, breeds, locations, x):
     assert "double u_a" in code and "u_a = (double)(sg_py_fmod((double)(5.5), (double)(2.0)));" in code
     assert "float u_b" in code and "sg_py_fmodf((float)(ctx.f32(PROP_x, (int)(sg_agent)))" in code
     assert "if (m != 0.0 && ((m < 0.0) != (b < 0.0))) m += b;" in code
+
+
+def test_min_max_of_several_values_and_math_constants():
+    """min/max fold left to right over any number of values; math.pi and
+    math.e are Python floats (weak: float32 with them stays float32)."""
+    src = '''
+def step(tick, agent_index, g, agent_ids, breeds, locations, x):
+    a = min(4, 2, 3)
+    b = max(x[agent_index], 0.5, cp.float32(0.25))
+    c = math.pi * 2
+    d = x[agent_index] * math.e
+'''
+    code, _, _ = translate_step(src, "step", ["g"], ["x"], {"x": "f"})
+    assert "long long u_a" in code and "float u_b" in code and "double u_c" in code and "float u_d" in code
+    assert "3.141592653589793" in code and "(float)(2.718281828459045)" in code
+    with pytest.raises(StepTranslationError, match="two or more"):
+        translate_step(src.replace("min(4, 2, 3)", "min(4)"), "step", ["g"], ["x"], {"x": "f"})

@@ -28,6 +28,7 @@ CASES = [
 FMOD = '''
 def fmod_step(tick, agent_index, d, agent_ids, breeds, locations, x, y):
     y[agent_index] = x[agent_index] % d + cp.float32(x[agent_index] % cp.float32(0.5))
+    y[agent_index] = max(y[agent_index], 0.0, min(d, math.pi, 4)) * math.e
 '''
 
 
