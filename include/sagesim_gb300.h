@@ -20,6 +20,8 @@
  *   sg_set_graph_csr              NetworkSpace adjacency -> CSR sagesim/space.py:107-125,
  *                                                               sagesim/internal_utils.py:111-186,
  *                                                               sagesim/model.py:1143-1148
+ *   sg_set_graph_id_edges         convert_agent_ids_to_indices  sagesim/model.py:31-110,
+ *                                 + CSR build (on the GPU)      sagesim/model.py:1068-1148
  *   sg_set_logical_ids            set_agent_logical_id          sagesim/model.py:656-667, 1089-1096
  *   sg_set_seed                   set_seed                      sagesim/model.py:652-654
  *   sg_set_globals_f64            register/set_global_property  sagesim/model.py:588-604
@@ -34,6 +36,9 @@
  *   sg_compile_step               register_step_func + codegen  sagesim/breed.py:68-99,
  *                                                               sagesim/model.py:2010-2457
  *   sg_run                        simulate -> worker_coroutine  sagesim/model.py:961-998, 1314-1640
+ *   sg_get_tick_history           per-tick S/I/R/E_S dumps      (no counterpart; the reference's
+ *                                                               tests read agents one by one,
+ *                                                               sagesim/model.py:422-450)
  */
 #ifndef SAGESIM_GB300_H
 #define SAGESIM_GB300_H
