@@ -10,13 +10,16 @@ ticks. One step = one simulate(200) from the initial state.
   e2e   : the same through the C ABI with host buffers (pinned): the initial
           state is copied in and the final state read back every step
   roofline : the dominant kernel's algorithmic bytes / its CUDA-event duration
-  cpu_baseline : the CPU port of the same tick (OpenMP, all host cores) on a
-                 bounded sample of ticks
+  parity_vs_oracle : every strategy's final state and per-tick S, I, R, E_S
+                 equal the oracle's run of the same 200 ticks
+  cpu_baseline : that oracle run (the C port of the reference tick, OpenMP on
+                 all host cores), one whole simulate(200), timed
 
 `--impl reference` times the reference's CPU implementation of this path. The
 reference runs its step only as a CuPy GPU kernel (its use_gpu=False flag is
 ignored), so its CPU implementation here is the C restatement of its tick in
-oracle/ on all host cores, on the same workload.
+oracle/ on all host cores, on the same workload: whole 200-tick runs, the
+input built by oracle/ alone (no engine library in that process).
 """
 import argparse
 import json
@@ -70,6 +73,20 @@ def build_workload(n=N_AGENTS):
     lids = np.empty(n, dtype=np.int64)
     lids[perm] = np.arange(n, dtype=np.int64)  # logical id = original agent id
     return roff, ridx, rst, lids
+
+
+def build_reference_workload(n=N_AGENTS):
+    """The same workload for the CPU reference arm, built by oracle/ only: the
+    Barabasi-Albert graph in generation order with logical id = agent id, which
+    is how SAGESim runs it on one rank (it has no locality relabel). The
+    engine's relabelled run keys every draw on the same logical ids, so both
+    give the same trajectory (agents permuted)."""
+    from oracle import oracle
+
+    off, idx = oracle.barabasi_albert(n, BA_M, SEED)
+    st = np.full(n, CODES[0], dtype=np.int32)
+    st[oracle.initial_infected(n, INFECTED_FRAC, SEED)] = CODES[1]
+    return off, idx, st
 
 
 class ClockSampler:
@@ -238,7 +255,20 @@ def ensemble_section(stream, steps, device=0, ticks=365):
             plain_ms += ev0.elapsed_time(ev1)
             mismatches += int(not np.array_equal(e.get_property(pr), fin))
             e.close()
+    # checker: a dozen scenarios, the two largest among them, against the oracle
+    from oracle import oracle
+
+    by_size = np.argsort([off.size for off, _ in gs], kind="stable")
+    pick = set(int(k) for k in by_size[-2:])
+    pick |= set(int(k) for k in np.random.default_rng(3).choice(len(gs), 10, replace=False))
+    oracle_ok = 0
+    for k in sorted(pick):
+        (off, idx), p = gs[k], params[k]
+        want, _, _ = oracle.sir_run(2, off, idx, states[k], p["seed"], 0, ticks, p["beta"], p["gamma"], CODES)
+        oracle_ok += int(np.array_equal(finals[k], want))
     return {"workload": "512 SIR scenarios (ER/BA/WS, n log-uniform 1e3..1e6, seed 3), 365 ticks",
+            "oracle_checked": {"scenarios": len(pick), "bit_exact": oracle_ok,
+                               "largest_agents": int(gs[int(by_size[-1])][0].size - 1)},
             "scenarios": len(gs), "agents": agents, "nnz": nnz, "graph_gen_s": gen_s,
             "batched_agent_ticks_per_s": agents * ticks / (batched_ms / 1e3), "batched_ms": batched_ms,
             "plain_sequential_agent_ticks_per_s": agents * ticks / (plain_ms / 1e3),
@@ -316,14 +346,19 @@ def opinion_section(stream, steps, device=0, peak=None, n=2_000_000, ticks=500):
     return out
 
 
-def serving_section(stream, device=0, n_requests=100, n_graphs=24):
-    """Config 5 scaled to n_requests: Poisson arrivals at 200 req/s (seed 4),
-    n log-uniform in [1e4, 5e6], BA or ER with mean degree 4..16, horizons
-    U{50..365}, 150 GB admission budget. Graph structures come from a pool of
-    n_graphs generated graphs; every request has its own seed, beta, gamma,
-    initial infections and horizon. The Poisson stream gives the latencies (its
-    throughput is bounded by the arrival rate); the same requests all arriving
-    at once give the served form's capacity (burst_*)."""
+def serving_section(stream, device=0, n_requests=1000, n_graphs=64):
+    """Config 5: a stream of n_requests requests, Poisson arrivals at 200 req/s
+    (seed 4), n log-uniform in [1e4, 5e6], BA or ER with mean degree 4..16,
+    horizons U{50..365}, 150 GB admission budget. Graph structures come from a
+    pool of n_graphs generated graphs; every fourth structure is relabelled by
+    a 16-way locality partition and its requests carry logical ids (the
+    original agent ids), so they must reproduce the run in the original order.
+    Every request has its own seed, beta, gamma, initial infections and
+    horizon. The Poisson stream gives the latencies (its throughput is bounded
+    by the arrival rate); the same requests all arriving at once give the
+    served form's capacity (burst_*). Every request's result is compared with
+    its run on the plain engine, and a sample (relabelled ones among them) with
+    the oracle run on the graph in its original order."""
     import torch
 
     from sagesim_gb300 import Engine, graphs
@@ -338,15 +373,35 @@ def serving_section(stream, device=0, n_requests=100, n_graphs=24):
             specs.append(("ba", n, max(2, int(round(deg / 2))), int(rng.integers(0, 2**62))))
         else:
             specs.append(("er", n, deg / (n - 1), int(rng.integers(0, 2**62))))
-    gs = graphs.generate_many(specs)
+    t0 = time.perf_counter()
+    base = graphs.generate_many(specs)
+    pool = []  # (offsets, indices, perm or None, lids or None) as requests see them
+    for g, (off, idx) in enumerate(base):
+        if g % 4 == 1:
+            perm, _ = graphs.partition_relabel(off, idx, 16, g)
+            roff, ridx = graphs.permute_csr(off, idx, perm)
+            lids = np.empty(off.size - 1, dtype=np.int64)
+            lids[perm] = np.arange(off.size - 1, dtype=np.int64)
+            pool.append((roff, ridx, perm, lids))
+        else:
+            pool.append((off, idx, None, None))
+    gen_s = time.perf_counter() - t0
     arrivals = np.cumsum(rng.exponential(1.0 / 200.0, size=n_requests))
-    reqs = []
+    reqs, gof, st_orig = [], [], []
     for i in range(n_requests):
-        off, idx = gs[int(rng.integers(0, n_graphs))]
+        g = int(rng.integers(0, n_graphs))
+        off, idx, perm, lids = pool[g]
         n = off.size - 1
-        reqs.append(dict(offsets=off, indices=idx, state=initial_state(n, 0.005, int(rng.integers(0, 2**31))),
-                         seed=int(rng.integers(0, 2**31)), beta=float(rng.uniform(0.01, 0.1)),
-                         gamma=float(rng.uniform(0.05, 0.2)), horizon=int(rng.integers(50, 366))))
+        st = initial_state(n, 0.005, int(rng.integers(0, 2**31)))  # in the original order
+        rst = st
+        if perm is not None:
+            rst = np.empty_like(st)
+            rst[perm] = st
+        gof.append(g)
+        st_orig.append(st)
+        reqs.append(dict(offsets=off, indices=idx, state=rst, seed=int(rng.integers(0, 2**31)),
+                         beta=float(rng.uniform(0.01, 0.1)), gamma=float(rng.uniform(0.05, 0.2)),
+                         horizon=int(rng.integers(50, 366)), lids=lids))
     with torch.cuda.stream(stream):
         srv = Server(budget_bytes=150 * 10**9, agent_slots=400_000_000, edge_slots=2_100_000_000,
                      max_resident=4096, variant="B", device=device, stream=stream.cuda_stream)
@@ -357,29 +412,57 @@ def serving_section(stream, device=0, n_requests=100, n_graphs=24):
                      max_resident=4096, variant="B", device=device, stream=stream.cuda_stream)
         burst = serve_stream(srv, reqs, np.zeros(n_requests), chunk=8, keep_results=False)
         srv.close()
-        # plain sequential: each request alone on the plain engine (device time)
+        # plain sequential: each request alone on the plain engine (device time of
+        # its simulate only); one engine per graph structure, its state, seed and
+        # probabilities set per request
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        plain_ms, mismatches, checked = 0.0, 0, 0
-        for i, r in enumerate(reqs):
+        plain_ms, mismatches = 0.0, 0
+        by_graph = {}
+        for i, g in enumerate(gof):
+            by_graph.setdefault(g, []).append(i)
+        for g, members in by_graph.items():
+            off, idx, _, lids = pool[g]
             e = Engine(device=device, stream=stream.cuda_stream)
-            e.set_graph(r["offsets"], r["indices"], symmetric=True)
-            e.set_seed(r["seed"])
-            pr = e.add_property("state", np.int32, init=r["state"])
-            e.add_sir(pr, r["beta"], r["gamma"], variant="B", strategy="count", codes=CODES)
-            stream.synchronize()
-            ev0.record(stream)
-            e.run_async(0, r["horizon"], use_graph=False)
-            ev1.record(stream)
-            stream.synchronize()
-            plain_ms += ev0.elapsed_time(ev1)
-            mismatches += int(not np.array_equal(e.get_property(pr), out["results"][i]))
-            checked += 1
+            e.set_graph(off, idx, symmetric=True)
+            if lids is not None:
+                e.set_logical_ids(lids)
+            pr = e.add_property("state", np.int32, init=reqs[members[0]]["state"])
+            sid = e.add_sir(pr, 0.1, 0.1, variant="B", strategy="count", codes=CODES)
+            for i in members:
+                r = reqs[i]
+                e.set_property(pr, r["state"])
+                e.set_seed(r["seed"])
+                e.update_sir(sid, pr, r["beta"], r["gamma"], variant="B", strategy="count", codes=CODES)
+                stream.synchronize()
+                ev0.record(stream)
+                e.run_async(0, r["horizon"], use_graph=False)
+                ev1.record(stream)
+                stream.synchronize()
+                plain_ms += ev0.elapsed_time(ev1)
+                mismatches += int(not np.array_equal(e.get_property(pr), out["results"][i]))
             e.close()
+    # checker: a sample of requests against the oracle on the graph in its original
+    # order (no logical ids); relabelled results are mapped back through perm
+    from oracle import oracle
+
+    sample = [i for i in range(n_requests) if pool[gof[i]][2] is not None][:4]
+    sample += [i for i in range(n_requests) if pool[gof[i]][2] is None][:4]
+    oracle_ok = 0
+    for i in sample:
+        off, idx = base[gof[i]]
+        perm = pool[gof[i]][2]
+        r = reqs[i]
+        want, _, _ = oracle.sir_run(2, off, idx, st_orig[i], r["seed"], 0, r["horizon"], r["beta"], r["gamma"],
+                                    CODES)
+        got = out["results"][i] if perm is None else out["results"][i][perm]
+        oracle_ok += int(np.array_equal(got, want))
     lat = out["latency_s"]
     agent_ticks = out["agent_ticks"]
     return {"workload": "%d SIR requests, Poisson 200 req/s (seed 4), n 1e4..5e6 log-uniform, BA/ER "
-                        "mean degree 4..16, horizons 50..365, 150 GB budget, %d graph structures"
-                        % (n_requests, n_graphs),
+                        "mean degree 4..16, horizons 50..365, 150 GB budget, %d graph structures (every "
+                        "fourth relabelled, its requests carrying logical ids)" % (n_requests, n_graphs),
+            "requests": n_requests, "with_logical_ids": int(sum(r["lids"] is not None for r in reqs)),
+            "graph_gen_s": gen_s,
             "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
             "served_agent_ticks_per_s": agent_ticks / out["wall_s"], "wall_s": out["wall_s"],
             "arrival_span_s": float(arrivals[-1]), "submit_s": out["submit_s"], "step_s": out["step_s"],
@@ -389,7 +472,9 @@ def serving_section(stream, device=0, n_requests=100, n_graphs=24):
             "burst_p50_latency_s": float(np.percentile(burst["latency_s"], 50)),
             "burst_p99_latency_s": float(np.percentile(burst["latency_s"], 99)),
             "plain_sequential_agent_ticks_per_s": agent_ticks / (plain_ms / 1e3),
-            "bit_exact_requests": checked - mismatches, "requests": n_requests}
+            "burst_vs_plain_sequential": (burst["agent_ticks"] / burst["wall_s"]) / (agent_ticks / (plain_ms / 1e3)),
+            "bit_exact_requests": n_requests - mismatches,
+            "oracle_checked": {"requests": len(sample), "bit_exact": oracle_ok}}
 
 
 def algorithmic_bytes(kernel, n, st0, tick_stats, active):
@@ -441,41 +526,37 @@ def algorithmic_bytes(kernel, n, st0, tick_stats, active):
     return np.array([4.0 * n + 12.0 * S_start[0] + 4.0 * E_S[0]])
 
 
-def cpu_port_rate(off, idx, st, lids, ticks, threads=0):
-    """Agent-ticks/s of the C port of the tick (oracle/) on the host cores."""
-    from oracle import oracle
-
-    oracle.lib()
-    t0 = time.perf_counter()
-    _, stats, _ = oracle.sir_run(2, off, idx, st, SEED, 0, ticks, BETA, GAMMA, CODES, lids=lids,
-                                 nthreads=threads)
-    dt = time.perf_counter() - t0
-    used = threads if threads > 0 else oracle.max_threads()
-    return (off.size - 1) * ticks / dt, dt, used, stats
-
-
 def run_reference(args):
+    """The reference arm: whole 200-tick runs of the C port of the reference
+    tick (oracle/, OpenMP on every host core), input built by oracle/ only.
+    One step = one simulate(200) from the initial state, timed on the host."""
     rank = _env_int("RANK", 0)
     if rank != 0:
         return
-    off, idx, st, lids = build_workload()
-    sample = max(1, _env_int("SG_REF_TICKS", 10))
-    rates = []
+    from oracle import oracle
+
+    off, idx, st = build_reference_workload()
+    used = oracle.max_threads()
     for _ in range(max(args.warmup, 0)):
-        cpu_port_rate(off, idx, st, lids, 1)
+        oracle.sir_run(2, off, idx, st, SEED, 0, TICKS, BETA, GAMMA, CODES)
+    times = []
     for _ in range(args.steps):
-        r, dt, used, _ = cpu_port_rate(off, idx, st, lids, sample)
-        rates.append(r)
-    v = float(np.median(rates))
+        t0 = time.perf_counter()
+        oracle.sir_run(2, off, idx, st, SEED, 0, TICKS, BETA, GAMMA, CODES)
+        times.append(time.perf_counter() - t0)
+    s_step = float(np.sum(times)) / max(len(times), 1)
+    v = N_AGENTS * TICKS / s_step
     line = {
         "impl": "reference", "metric": "SIR agent-ticks/s (BA 1e7, 200-tick simulate)", "value": v,
         "unit": "agent-ticks/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": N_AGENTS * TICKS / v * 1e3, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": s_step * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": WORKLOAD % N_AGENTS, "sample": "%d ticks per step from tick 0" % sample},
+        "config": {"workload": WORKLOAD % N_AGENTS,
+                   "order": "graph in generation order, logical id = agent id (the relabel is the engine's "
+                            "layout; same trajectory)"},
         "cpu_baseline": {"value": v, "unit": "agent-ticks/s", "cores": used, "kind": "port",
-                         "sample": "%d ticks of the 200-tick run per step (C port of the reference "
-                                   "tick, OpenMP)" % sample},
+                         "sample": "whole 200-tick simulate per step, %d steps (C port of the reference "
+                                   "tick, OpenMP)" % args.steps},
         "e2e": {"value": v, "unit": "agent-ticks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -524,48 +605,6 @@ def profile_opinion(args):
     print("opinion profile case done: %d agents, 30 ticks, mean opinion %.6f" % (n, float(out.mean())))
 
 
-def sweep(args):
-    """Device time of simulate(200) for every count-step launch configuration."""
-    import torch
-
-    from sagesim_gb300 import Engine
-
-    off, idx, st0, lids = build_workload(args.agents)
-    stream = torch.cuda.Stream()
-    rows = []
-    with torch.cuda.stream(stream):
-        eng = Engine(stream=stream.cuda_stream)
-        eng.set_graph(off, idx, symmetric=True)
-        eng.set_logical_ids(lids)
-        eng.set_seed(SEED)
-        prop = eng.add_property("state", np.int32, init=st0)
-        eng.add_sir(prop, BETA, GAMMA, variant="B", strategy="count", codes=CODES)
-        eng.snapshot()
-        ref = None
-        for bps in (8, 16):
-            for fl in (0, 2, 3, 4, 5, 16, 24, 16 | 256, 16 | 256 | 2, 16 | 256 | 3, 16 | 256 | 4, 16 | 256 | 5,
-                       16 | 256 | 6):
-                eng.set_tune(blocks_per_sm=bps, count_flavour=fl)
-                for _ in range(2):
-                    eng.restore()
-                    eng.run_async(0, TICKS)
-                stream.synchronize()
-                ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                ev0.record(stream)
-                for _ in range(5):
-                    eng.restore()
-                    eng.run_async(0, TICKS)
-                ev1.record(stream)
-                stream.synchronize()
-                fin = eng.get_property(prop)
-                ref = fin if ref is None else ref
-                rows.append({"blocks_per_sm": bps, "count_flavour": fl, "ms_per_step": ev0.elapsed_time(ev1) / 5,
-                             "same_result": bool(np.array_equal(fin, ref))})
-        eng.close()
-    for r in sorted(rows, key=lambda r: r["ms_per_step"]):
-        print(json.dumps(r))
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -578,8 +617,6 @@ def main():
                     help="with --profile-case: collect and print per-tick S/I/R/E_S")
     ap.add_argument("--flavour", type=int, default=-1, help="count-step flavour for --profile-case")
     ap.add_argument("--bps", type=int, default=16, help="blocks per SM for --profile-case")
-    ap.add_argument("--sweep", action="store_true",
-                    help="time every count-step flavour x blocks/SM on the workload and exit")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the ensemble and serving sections")
     ap.add_argument("--profile-opinion", action="store_true",
@@ -595,9 +632,6 @@ def main():
         return
     if args.profile_opinion:
         profile_opinion(args)
-        return
-    if args.sweep:
-        sweep(args)
         return
 
     import torch
@@ -709,16 +743,30 @@ def main():
                          "kernel_bytes_per_launch": own, "kernel_achieved": own_achieved,
                          "kernel_frac": own_achieved / peak},
             "kernels": {k: {"launches": v[0], "total_ms": v[1]} for k, v in rep.items()},
-            "clocks": clocks, "final": final,
+            "clocks": clocks, "final": final, "tick_stats": tick_stats,
         }
 
     results = {}
     for strategy in [args.strategy] + [s for s in ("count", "frontier", "pull") if s != args.strategy]:
         results[strategy] = measure(strategy, args.steps, args.warmup)
     head = results[args.strategy]
-    for s_, r_ in results.items():
-        if not np.array_equal(r_["final"], head["final"]):
-            raise RuntimeError("strategies disagree on the final state")
+
+    # checker: the oracle runs the same 200 ticks on the host cores (rank 0); every
+    # strategy's final state and per-tick S, I, R, E_S must equal it. The run is
+    # timed: it is the CPU baseline (one whole simulate(200)).
+    parity, cpu = None, None
+    if rank == 0:
+        from oracle import oracle
+
+        t0 = time.perf_counter()
+        want, want_stats, _ = oracle.sir_run(2, off, idx, st0, SEED, 0, TICKS, BETA, GAMMA, CODES, lids=lids)
+        cpu_s = time.perf_counter() - t0
+        parity = {s_: {"final_state": bool(np.array_equal(r_["final"], want)),
+                       "tick_stats": bool(np.array_equal(r_["tick_stats"], want_stats))}
+                  for s_, r_ in results.items()}
+        cpu = {"value": n * TICKS / cpu_s, "unit": "agent-ticks/s", "cores": oracle.max_threads(), "kind": "port",
+               "sample": "one whole 200-tick simulate of the same workload (%.2f s), C port of the reference "
+                         "tick (oracle/), OpenMP" % cpu_s}
 
     extra = {}
     if rank == 0 and not args.no_extras:
@@ -729,14 +777,6 @@ def main():
                 extra[name] = fn()
             except Exception as exc:  # a failing extra section must not lose the headline line
                 extra[name] = {"error": "%s: %s" % (type(exc).__name__, exc)}
-
-    cpu = None
-    if rank == 0:
-        sample = max(1, _env_int("SG_CPU_TICKS", 10))
-        rate, dt, used, _ = cpu_port_rate(off, idx, st0, lids, sample)
-        cpu = {"value": rate, "unit": "agent-ticks/s", "cores": used, "kind": "port",
-               "sample": "first %d ticks of the same workload (%.1f s), C port of the reference tick "
-                         "(oracle/), OpenMP" % (sample, dt)}
 
     line = {
         "metric": "SIR agent-ticks/s (BA 1e7, 200-tick simulate)", "value": head["value"],
@@ -755,7 +795,10 @@ def main():
         "kernels": head["kernels"],
         "clocks": head["clocks"],
         "cpu_baseline": cpu,
-        "strategies": {k: {kk: vv for kk, vv in v.items() if kk not in ("final", "clocks")}
+        "parity_vs_oracle": None if parity is None else all(p["final_state"] and p["tick_stats"]
+                                                             for p in parity.values()),
+        "parity_detail": parity,
+        "strategies": {k: {kk: vv for kk, vv in v.items() if kk not in ("final", "clocks", "tick_stats")}
                        for k, v in results.items()},
     }
     line.update(extra)

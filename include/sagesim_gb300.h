@@ -344,10 +344,13 @@ typedef struct sg_server_cfg {
 int sg_server_create(const sg_server_cfg *cfg, sg_server **out);
 int sg_server_destroy(sg_server *s);
 int sg_server_last_error(const sg_server *s, char *buf, size_t cap);
-/* Submits a request; the CSR must be symmetric. With nothing queued and room in
- * the budget and pool it is placed on the device at once (status RUNNING; the
- * CSR is checked there), else queued (the host arrays are checked and copied).
- * Either way the caller's arrays are free again when the call returns. */
+/* Submits a request; the CSR must be symmetric. d->lids (nullable) gives each
+ * agent's logical id, the key of its draws (sagesim/model.py:656-667), so a
+ * request relabelled for locality reproduces its run in the original order.
+ * With nothing queued and room in the budget and pool it is placed on the
+ * device at once (status RUNNING; the CSR is checked there), else queued (the
+ * host arrays are checked and copied). Either way the caller's arrays are free
+ * again when the call returns. */
 int sg_server_submit(sg_server *s, const sg_scenario_desc *d, int64_t *rid);
 /* Admits, runs nticks for every resident scenario, retires the finished ones.
  * Synchronous. n_done (nullable) = requests finished by this step. */

@@ -52,6 +52,8 @@ def lib():
         L.sgo_normal_batch.restype = None
         L.sgo_normal_batch.argtypes = [_i64, _p, _p, _p, _p, _p]
         L.sgo_max_threads.restype = ctypes.c_int
+        L.sgo_graph_ba.restype = ctypes.c_int
+        L.sgo_graph_ba.argtypes = [_i64, _i32, ctypes.c_uint64, _p, _p, ctypes.POINTER(_i64)]
         _lib = L
     return _lib
 
@@ -128,3 +130,24 @@ def opinion_run(offsets, indices, weights, opinion, seed, tick0, nticks, sigma, 
 
 def max_threads():
     return int(lib().sgo_max_threads())
+
+
+def barabasi_albert(n, m, seed):
+    """Symmetric int32 CSR of the seeded Barabasi-Albert graph (sgo_graph_ba)."""
+    nnz = _i64()
+    rc = lib().sgo_graph_ba(int(n), int(m), int(seed) & (2**64 - 1), None, None, ctypes.byref(nnz))
+    if rc != 0:
+        raise ValueError("sgo_graph_ba: bad arguments")
+    off = np.empty(int(n) + 1, dtype=np.int32)
+    idx = np.empty(max(nnz.value, 1), dtype=np.int32)
+    rc = lib().sgo_graph_ba(int(n), int(m), int(seed) & (2**64 - 1), _ptr(off), _ptr(idx), ctypes.byref(nnz))
+    if rc != 0:
+        raise MemoryError("sgo_graph_ba: out of memory")
+    return off, idx[:nnz.value]
+
+
+def initial_infected(n, fraction, seed):
+    """Indices of round(fraction * n) distinct agents drawn by numpy's PCG64
+    generator (the same draw the engine's input helpers make)."""
+    k = int(round(fraction * n))
+    return np.sort(np.random.default_rng(seed).choice(n, size=k, replace=False)).astype(np.int64)

@@ -220,6 +220,133 @@ int sgo_opinion_run(int64_t n, const int32_t *off, const int32_t *idx, const int
     return 0;
 }
 
+/* ---- input generator for the CPU baseline -------------------------------
+ * The reference builds its graphs in user code (networkx, e.g.
+ * scaling_tests/weak_scaling_sir.py builds its SIR graphs before timing
+ * simulate()); networkx takes minutes and tens of GB at 10^7 agents, so the
+ * benchmark's Barabasi-Albert input is written out here from its published
+ * definition, so that the CPU baseline builds its input without the engine's
+ * library. The stream is xoshiro256** seeded through splitmix64 (Blackman &
+ * Vigna), bounded draws by Lemire's multiply-shift rejection method; the
+ * attachment rule is the usual linear preferential attachment: node m joins
+ * nodes 0..m-1, every later node t joins m distinct nodes drawn uniformly
+ * from the list of all edge endpoints so far (repeats redrawn). Rows list
+ * neighbours in edge order. The engine's generator follows the same
+ * definition; a CPU test checks that both give the same CSR. */
+typedef struct { uint64_t s[4]; } sgo_xoshiro;
+
+static void sgo_xoshiro_seed(sgo_xoshiro *r, uint64_t seed)
+{
+    uint64_t z = seed;
+    for (int k = 0; k < 4; ++k) {
+        z += 0x9E3779B97F4A7C15ULL;
+        uint64_t x = z;
+        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+        r->s[k] = x ^ (x >> 31);
+    }
+}
+
+static inline uint64_t sgo_rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+static uint64_t sgo_xoshiro_next(sgo_xoshiro *r)
+{
+    uint64_t *s = r->s;
+    const uint64_t out = sgo_rotl(s[1] * 5, 7) * 9;
+    const uint64_t t = s[1] << 17;
+    s[2] ^= s[0];
+    s[3] ^= s[1];
+    s[1] ^= s[2];
+    s[0] ^= s[3];
+    s[2] ^= t;
+    s[3] = sgo_rotl(s[3], 45);
+    return out;
+}
+
+static uint64_t sgo_below(sgo_xoshiro *r, uint64_t bound)
+{
+    if (bound <= 1) return 0;
+    const uint64_t reject_below = (0 - bound) % bound;
+    for (;;) {
+        const unsigned __int128 m = (unsigned __int128)sgo_xoshiro_next(r) * bound;
+        if ((uint64_t)m >= reject_below) return (uint64_t)(m >> 64);
+    }
+}
+
+/* Barabasi-Albert graph as a symmetric CSR. Call with offsets == NULL to get
+ * nnz only, then again with offsets[n+1] and indices[nnz]. Returns 0, -1 on a
+ * bad argument, -2 when out of memory. */
+int sgo_graph_ba(int64_t n, int32_t m, uint64_t seed, int32_t *offsets, int32_t *indices, int64_t *nnz)
+{
+    if (n < 0 || n >= INT32_MAX || m < 1 || !nnz) return -1;
+    if (n <= m) {
+        *nnz = 0;
+        if (offsets) memset(offsets, 0, (size_t)(n + 1) * sizeof(int32_t));
+        return 0;
+    }
+    const int64_t nedges = (n - m) * (int64_t)m;
+    if (2 * nedges >= INT32_MAX) return -1;
+    *nnz = 2 * nedges;
+    if (!offsets) return 0;
+    /* edge k joins src[k] = m + k / m to dst[k]; endpoints list for the draws */
+    int32_t *dst = (int32_t *)malloc((size_t)nedges * sizeof(int32_t));
+    int32_t *ends = (int32_t *)malloc((size_t)(2 * nedges) * sizeof(int32_t));
+    int64_t *stamp = (int64_t *)malloc((size_t)n * sizeof(int64_t));
+    int32_t *tgt = (int32_t *)malloc((size_t)m * sizeof(int32_t));
+    if (!dst || !ends || !stamp || !tgt) {
+        free(dst); free(ends); free(stamp); free(tgt);
+        return -2;
+    }
+    for (int64_t i = 0; i < n; ++i) stamp[i] = -1;
+    for (int32_t k = 0; k < m; ++k) tgt[k] = k;
+    sgo_xoshiro rng;
+    sgo_xoshiro_seed(&rng, seed);
+    int64_t ne = 0, nend = 0;
+    for (int64_t t = m; t < n; ++t) {
+        for (int32_t k = 0; k < m; ++k) {
+            dst[ne++] = tgt[k];
+            ends[nend++] = (int32_t)t;
+            ends[nend++] = tgt[k];
+        }
+        if (t + 1 < n) {
+            int32_t got = 0;
+            while (got < m) {
+                const int32_t c = ends[sgo_below(&rng, (uint64_t)nend)];
+                if (stamp[c] == t) continue;
+                stamp[c] = t;
+                tgt[got++] = c;
+            }
+        }
+    }
+    free(ends);
+    free(stamp);
+    free(tgt);
+    /* rows in edge order: edge (t, d) appends d to row t and t to row d; the
+     * m targets of a node are distinct, so no pair repeats */
+    memset(offsets, 0, (size_t)(n + 1) * sizeof(int32_t));
+    for (int64_t k = 0; k < nedges; ++k) {
+        offsets[m + k / m + 1]++;
+        offsets[dst[k] + 1]++;
+    }
+    for (int64_t i = 0; i < n; ++i) offsets[i + 1] += offsets[i];
+    if (indices) {
+        int32_t *cur = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+        if (!cur) {
+            free(dst);
+            return -2;
+        }
+        memcpy(cur, offsets, (size_t)n * sizeof(int32_t));
+        for (int64_t k = 0; k < nedges; ++k) {
+            const int32_t s = (int32_t)(m + k / m), d = dst[k];
+            indices[cur[s]++] = d;
+            indices[cur[d]++] = s;
+        }
+        free(cur);
+    }
+    free(dst);
+    return 0;
+}
+
 /* Bulk RNG helpers for vector checks. */
 void sgo_philox_batch(int64_t count, const int64_t *seed, const int64_t *tick,
                       const int64_t *lid, const int64_t *salt, uint32_t *k23_out)

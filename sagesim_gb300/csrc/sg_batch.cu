@@ -285,9 +285,12 @@ int SgPool::place(const sg_scenario_desc &d, const int32_t *loff, const int32_t 
     s.kinf = sg_threshold_host(d.beta);
     s.krec = sg_threshold_host(d.gamma);
     s.symmetric = sym;
-    if (any_lids) {
+    // a scenario without logical ids keys its draws on the local index, which
+    // the kernels derive from the segment's base (its segment has no lids)
+    s.has_lids = llids != nullptr;
+    if (llids) {
         std::vector<uint32_t> k((size_t)n);
-        for (int64_t i = 0; i < n; ++i) k[(size_t)i] = llids ? (uint32_t)(uint64_t)llids[i] : (uint32_t)i;
+        for (int64_t i = 0; i < n; ++i) k[(size_t)i] = (uint32_t)(uint64_t)llids[i];
         POOL_CK(cudaMemcpyAsync(lids.as<uint32_t>() + ab, k.data(), (size_t)n * 4, cudaMemcpyHostToDevice, stream));
     }
     // long rows (candidates for whole-block scans), in index order; large
@@ -365,7 +368,7 @@ int SgPool::upload_segs()
         memset(&g, 0, sizeof g);
         g.tick0 = s.tick;
         g.end_tick = s.horizon;
-        g.lids = any_lids ? lids.as<uint32_t>() : nullptr;
+        g.lids = any_lids && s.has_lids ? lids.as<uint32_t>() : nullptr;
         g.lid_base = (int32_t)s.agent_base;
         g.variant = builtin;
         g.key = s.key;

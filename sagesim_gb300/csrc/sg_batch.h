@@ -130,6 +130,7 @@ struct SgPoolScen {
     sg_scenario_desc d{}; // host pointers are not kept
     uint32_t key = 0, kinf = 0, krec = 0;
     std::vector<uint32_t> lids; // empty: lid = local index
+    bool has_lids = false;      // keys in the pool's logical-id array (else the local index)
     bool symmetric = true;
 };
 

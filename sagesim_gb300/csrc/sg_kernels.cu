@@ -538,9 +538,28 @@ cudaError_t sg_launch_sir_pull(const SgTickArgs &a, int variant, bool stats, int
     return cudaGetLastError();
 }
 
+// SM count of the current device: grids of the grid-stride kernels below are
+// sized as a multiple of it.
+static int current_sm_count()
+{
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+        v = 1; // the launch that follows reports the device's error
+    return v;
+}
+
+// Blocks of 256 threads for `work` items, at most 16 per SM (grid-stride loops).
+static int stride_grid(int64_t work)
+{
+    const int64_t cap = (int64_t)current_sm_count() * 16;
+    const int64_t b = (work + 255) / 256;
+    return (int)(b < 1 ? 1 : b > cap ? cap : b);
+}
+
 cudaError_t sg_launch_opinion_tables(double *radius, double *cosine, cudaStream_t st)
 {
-    opinion_tables_kernel<<<152 * 8, 256, 0, st>>>(radius, cosine);
+    opinion_tables_kernel<<<current_sm_count() * 8, 256, 0, st>>>(radius, cosine);
     return cudaGetLastError();
 }
 
@@ -574,8 +593,7 @@ cudaError_t sg_launch_offset_csr(int32_t *off, int64_t n1, int32_t edge_base, in
 {
     const int64_t work = n1 > nnz ? n1 : nnz;
     if (work <= 0) return cudaSuccess;
-    int64_t blocks = (work + 255) / 256;
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    const int blocks = stride_grid(work);
     offset_csr_kernel<<<(int)blocks, 256, 0, st>>>(off, n1, edge_base, idx, nnz, agent_base);
     return cudaGetLastError();
 }
@@ -585,8 +603,7 @@ cudaError_t sg_launch_check_csr(const int32_t *off, int64_t n, const int32_t *id
 {
     const int64_t work = n > nnz ? n : nnz;
     if (work <= 0) return cudaSuccess;
-    int64_t blocks = (work + 255) / 256;
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    const int blocks = stride_grid(work);
     check_csr_kernel<<<(int)blocks, 256, 0, st>>>(off, n, idx, nnz, flag);
     return cudaGetLastError();
 }
@@ -594,8 +611,7 @@ cudaError_t sg_launch_check_csr(const int32_t *off, int64_t n, const int32_t *id
 cudaError_t sg_launch_copy_words(const uint32_t *src, uint32_t *dst, int64_t n, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
-    int64_t blocks = (n + 255) / 256;
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    const int blocks = stride_grid(n);
     copy_words_kernel<<<(int)blocks, 256, 0, st>>>(src, dst, n);
     return cudaGetLastError();
 }
@@ -615,8 +631,7 @@ cudaError_t sg_transpose_csr(const int32_t *off, const int32_t *idx, int64_t n, 
     cudaError_t err = cudaMemsetAsync(tmp, 0, (size_t)(n + 1) * sizeof(int32_t), st);
     if (err != cudaSuccess) return err;
     if (nnz > 0) {
-        int64_t blocks = (nnz + 255) / 256;
-        if (blocks > 152 * 16) blocks = 152 * 16;
+        const int blocks = stride_grid(nnz);
         degree_count_kernel<<<(int)blocks, 256, 0, st>>>(idx, nnz, tmp);
         if ((err = cudaGetLastError()) != cudaSuccess) return err;
     }
@@ -627,8 +642,7 @@ cudaError_t sg_transpose_csr(const int32_t *off, const int32_t *idx, int64_t n, 
     err = cudaMemcpyAsync(tmp, toff, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
     if (err != cudaSuccess) return err;
     if (n > 0) {
-        int64_t blocks = (n + 255) / 256;
-        if (blocks > 152 * 16) blocks = 152 * 16;
+        const int blocks = stride_grid(n);
         transpose_fill_kernel<<<(int)blocks, 256, 0, st>>>(off, idx, n, tmp, tidx);
         err = cudaGetLastError();
     }

@@ -16,10 +16,13 @@
 // (different streams, no ordering between them) race on it and give wrong
 // results. Calls issued on one stream, or otherwise ordered, are safe; each
 // call clears the part of the array it reads before reading it.
+#include <cuda.h> // CUcontext / CUresult types only; the calls go through entry points
 #include <cuda_runtime.h>
 
 #include <mutex>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "../../include/sagesim_gb300.h"
 #include "sg_kernels.h"
@@ -43,32 +46,80 @@ static_assert(kEnd <= SG_NOALLOC_SCRATCH_BYTES, "scratch layout exceeds the decl
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[SG_NOALLOC_SCRATCH_BYTES];
 
-// Device address of g_noalloc_scratch per device. In host code the symbol
-// name is only a host-side stand-in, so the address is looked up once per
-// device with that device current and handed to the kernels.
-std::mutex g_mu;
-void *g_scratch[256] = {};
+// Device address of g_noalloc_scratch per CUDA context. In host code the
+// symbol name is only a host-side stand-in, so the address is looked up with
+// cudaGetSymbolAddress once per context, with that context's device current,
+// and handed to the kernels. The cache is keyed on the context's unique id
+// (cuCtxGetId), not on the device number: after cudaDeviceReset, or with a
+// non-primary context current, the id differs and the address is looked up
+// again instead of reusing one that belongs to another (or a destroyed)
+// context. The two driver calls are reached through the runtime's
+// driver-entry-point lookup, so the library still links no driver library.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
 
-int scratch_for_current_device(void **out)
+std::mutex g_mu;
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+std::vector<std::pair<unsigned long long, void *>> g_scratch; // context id -> device address
+
+int noalloc_fail(const char *what, cudaError_t ce)
+{
+    sg_set_thread_error(std::string("sg_sir_run_noalloc: ") + what + ": " + cudaGetErrorString(ce));
+    return SG_ERR_CUDA;
+}
+
+// Id of the current context; 0 when none is current yet. Called with g_mu held.
+int current_context_id(unsigned long long *id)
+{
+    *id = 0;
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+        cudaError_t ce = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", (void **)&g_ctx_get_current, 12000,
+                                                          cudaEnableDefault, &q1);
+        if (ce == cudaSuccess)
+            ce = cudaGetDriverEntryPointByVersion("cuCtxGetId", (void **)&g_ctx_get_id, 12000, cudaEnableDefault,
+                                                  &q2);
+        if (ce != cudaSuccess || q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess ||
+            !g_ctx_get_current || !g_ctx_get_id) {
+            g_ctx_get_current = nullptr;
+            g_ctx_get_id = nullptr;
+            return noalloc_fail("driver entry points cuCtxGetCurrent / cuCtxGetId", ce);
+        }
+    }
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS) return noalloc_fail("cuCtxGetCurrent", cudaErrorUnknown);
+    if (!ctx) return SG_OK;
+    if (g_ctx_get_id(ctx, id) != CUDA_SUCCESS) return noalloc_fail("cuCtxGetId", cudaErrorUnknown);
+    return SG_OK;
+}
+
+int scratch_for_current_context(void **out)
 {
     int dev = -1;
     cudaError_t ce = cudaGetDevice(&dev);
-    if (ce != cudaSuccess || dev < 0 || dev >= 256) {
-        sg_set_thread_error(std::string("sg_sir_run_noalloc: cudaGetDevice: ") + cudaGetErrorString(ce));
-        return SG_ERR_CUDA;
-    }
+    if (ce != cudaSuccess || dev < 0) return noalloc_fail("cudaGetDevice", ce);
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch[dev]) {
-        void *p = nullptr;
-        ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (ce != cudaSuccess || !p) {
-            sg_set_thread_error(std::string("sg_sir_run_noalloc: cudaGetSymbolAddress: ") +
-                                cudaGetErrorString(ce));
-            return SG_ERR_CUDA;
-        }
-        g_scratch[dev] = p;
+    unsigned long long id = 0;
+    int rc = current_context_id(&id);
+    if (rc) return rc;
+    if (id)
+        for (const auto &e : g_scratch)
+            if (e.first == id) {
+                *out = e.second;
+                return SG_OK;
+            }
+    // first call in this context (or no context current yet: the lookup makes
+    // the device's primary context current)
+    void *p = nullptr;
+    ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (ce != cudaSuccess || !p) return noalloc_fail("cudaGetSymbolAddress", ce);
+    if (!id) {
+        rc = current_context_id(&id);
+        if (rc) return rc;
     }
-    *out = g_scratch[dev];
+    if (id) g_scratch.emplace_back(id, p);
+    *out = p;
     return SG_OK;
 }
 
@@ -112,7 +163,7 @@ extern "C" int sg_sir_run_noalloc(const int32_t *d_offsets, const int32_t *d_ind
         return SG_ERR_INVALID;
     }
     void *base = nullptr;
-    int rc = scratch_for_current_device(&base);
+    int rc = scratch_for_current_context(&base);
     if (rc != SG_OK) return rc;
     unsigned char *b = static_cast<unsigned char *>(base);
     cudaStream_t st = (cudaStream_t)stream;
@@ -144,9 +195,9 @@ extern "C" int sg_sir_run_noalloc(const int32_t *d_offsets, const int32_t *d_ind
     int sms = 0;
     if (ce == cudaSuccess) {
         int dev = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
-            sms = 152;
+        ce = cudaGetDevice(&dev);
+        if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (ce == cudaSuccess && sms <= 0) ce = cudaErrorInvalidDevice;
     }
     SgTickArgs a{};
     a.off = d_offsets;

@@ -124,7 +124,8 @@ int sg_server_create(const sg_server_cfg *cfg, sg_server **out)
     s->cfg = *cfg;
     sg_engine_cfg ec{cfg->device, 0, cfg->stream};
     int rc = s->pool.init(&ec);
-    if (!rc) rc = s->pool.allocate(cfg->agent_slots, cfg->edge_slots, cfg->max_resident, false, false);
+    // the pool keeps a logical-id array, so a request may carry its own RNG keys
+    if (!rc) rc = s->pool.allocate(cfg->agent_slots, cfg->edge_slots, cfg->max_resident, false, true);
     if (rc) {
         sg_set_thread_error(s->pool.err);
         s->pool.destroy();
@@ -163,11 +164,10 @@ int sg_server_submit(sg_server *s, const sg_scenario_desc *d, int64_t *rid)
     if (d->n_agents < 0 || d->nnz < 0 || !d->offsets || (d->nnz > 0 && !d->indices))
         return s->pool.fail(SG_ERR_INVALID, "bad CSR sizes or NULL arrays");
     if (!d->state && d->n_agents > 0) return s->pool.fail(SG_ERR_INVALID, "state is NULL");
-    const int64_t bytes = sg_pool_scenario_bytes(d->n_agents, d->nnz, false, false);
+    const int64_t bytes = sg_pool_scenario_bytes(d->n_agents, d->nnz, false, d->lids != nullptr);
     if (bytes > s->cfg.budget_bytes || d->n_agents + 1 > s->cfg.agent_slots || d->nnz > s->cfg.edge_slots)
         return s->pool.fail(SG_ERR_BUDGET, "request needs " + std::to_string((long long)bytes) +
                                                " bytes / slots beyond the server's budget or pool");
-    if (d->lids) return s->pool.fail(SG_ERR_INVALID, "the server keys the RNG on local agent indices");
     if (d->offsets[0] != 0 || d->offsets[d->n_agents] != d->nnz)
         return s->pool.fail(SG_ERR_BAD_CSR, "offsets must start at 0 and end at nnz");
     // Nothing queued ahead and room now: placed on the device at once, straight
@@ -176,7 +176,7 @@ int sg_server_submit(sg_server *s, const sg_scenario_desc *d, int64_t *rid)
     if (s->queue.empty() && s->resident_bytes + bytes <= s->cfg.budget_bytes &&
         s->pool.fits(d->n_agents, d->nnz)) {
         const int32_t sid = s->next_sid++;
-        const int rc = s->pool.place(*d, d->offsets, d->indices, d->state, nullptr, sid, true);
+        const int rc = s->pool.place(*d, d->offsets, d->indices, d->state, d->lids, sid, true);
         if (rc == SG_OK) {
             auto r = std::make_unique<Request>();
             r->rid = s->next_rid++;
@@ -202,6 +202,7 @@ int sg_server_submit(sg_server *s, const sg_scenario_desc *d, int64_t *rid)
     r->off.assign(d->offsets, d->offsets + d->n_agents + 1);
     r->idx.assign(d->indices, d->indices + d->nnz);
     r->state.assign(d->state, d->state + d->n_agents);
+    if (d->lids) r->lids.assign(d->lids, d->lids + d->n_agents);
     r->d.offsets = r->d.indices = r->d.state = nullptr;
     r->d.lids = nullptr;
     r->bytes = bytes;

@@ -148,10 +148,16 @@ __global__ void low_word_kernel(const unsigned long long *k, long long m, int32_
         idx[i] = (int32_t)(k[i] & 0xFFFFFFFFull);
 }
 
+// Blocks of 256 threads for `work` items, at most 16 per SM of the current
+// device (grid-stride loops).
 int grid_of(long long work)
 {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        sms = 1; // the launch that follows reports the device's error
     const long long b = (work + 255) / 256;
-    return (int)std::max<long long>(1, std::min<long long>(b, 152 * 16));
+    return (int)std::max<long long>(1, std::min<long long>(b, (long long)sms * 16));
 }
 
 struct Buf {

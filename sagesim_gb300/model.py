@@ -239,10 +239,34 @@ class Model:
                 integral = vals.dtype.kind in "iub" or (
                     vals.dtype.kind == "f" and vals.size and np.all(np.isfinite(vals)) and
                     np.all(vals == np.round(vals)) and not isinstance(default, float))
+                if integral and vals.size:
+                    integral = bool(np.all(vals >= -2**31) and np.all(vals < 2**31))
                 if integral:
                     self._props[name] = (np.int32, 1, vals.astype(np.int32)[order])
                 else:
                     self._props[name] = (np.float32, 1, vals.astype(np.float32)[order])
+        self._settle_written_types()
+
+    def _settle_written_types(self):
+        """The reference keeps every property in float32 (sagesim/internal_utils.py:
+        189-230, sagesim/model.py:1085), so a step may store a fraction into a
+        property that started as whole numbers. A property inferred as int32 stays
+        int32 only when no Python-dialect step writes it, or when a builtin SIR
+        step (whose state is int32) does; otherwise it is float32, as in the
+        reference."""
+        py_written, sir_written = set(), set()
+        gnames = [k for k, _ in sorted(self._global_names.items(), key=lambda kv: kv[1])]
+        arrays = [(b["name"], b["shape_per_agent"]) for b in self._breed_local_arrays]
+        widths = {k: v[1] for k, v in self._props.items()}
+        for _, _, fn, _ in self._steps:
+            if isinstance(fn, PythonStep):
+                py_written |= fn.written(gnames, list(self._props), arrays, widths)
+            elif isinstance(fn, SIRStep):
+                sir_written.add(fn.state)
+        for name in sorted(py_written - sir_written):
+            if name in self._props and self._props[name][0] == np.int32:
+                dt, width, arr = self._props[name]
+                self._props[name] = (np.float32, width, arr.astype(np.float32))
 
     def _global_offsets(self):
         offs, flat = {}, []

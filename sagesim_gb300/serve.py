@@ -50,9 +50,12 @@ class Server:
     def __exit__(self, *exc):
         self.close()
 
-    def submit(self, offsets, indices, state, seed, beta, gamma, horizon, codes=(1, 2, 3)):
+    def submit(self, offsets, indices, state, seed, beta, gamma, horizon, codes=(1, 2, 3), lids=None):
+        """Queues (or places at once) one scenario. lids: the logical id of every
+        agent, the key of its random draws (sagesim/model.py:656-667); None keys
+        the draws on the agent index, as the reference does by default."""
         keep = []
-        d = scenario_desc(offsets, indices, state, seed, beta, gamma, self.variant, horizon, None, codes,
+        d = scenario_desc(offsets, indices, state, seed, beta, gamma, self.variant, horizon, lids, codes,
                           True, keep)
         rid = ctypes.c_int64()
         self._ck(self._lib.sg_server_submit(self._h, ctypes.byref(d), ctypes.byref(rid)))

@@ -96,6 +96,16 @@ class PythonStep:
         self._writes = tuple(writes)
         return CudaStep(src, entry, writes=list(writes))
 
+    def written(self, globals_, props, arrays=(), prop_widths=None):
+        """Names of the properties and arrays the step writes, found before the
+        property types are settled (the step is translated once with every
+        property taken as float32; only its casts depend on that)."""
+        from .translate import translate_step
+
+        _, _, writes = translate_step(self.source, self.name, globals_, props, {p: "f" for p in props},
+                                      arrays=arrays, prop_widths=prop_widths)
+        return set(writes)
+
     @property
     def writes(self):
         if self._writes is None:

@@ -30,6 +30,13 @@ Outputs (committed; the tests read only these files):
                        properties read through row aliases), 25 ticks
   helpers_er.npz       1,000-agent ER graph, per-neighbour SIR written with the
                        device helpers of sagesim/utils.py, 30 ticks
+  fraction_er.npz      1,500-agent ER graph, SIR with two properties that start
+                       as whole numbers and are written fractions (immunity,
+                       load), 25 ticks
+  binding_er.npz       the INTEGRATION.md binding's extraction (GB300SIRModel.
+                       gb300_inputs) of a 2,000-agent ER SIR model with some
+                       logical ids, and the reference pipeline's own states of
+                       that model after every one of 30 ticks
   opinion_ws.npz       2,000-agent WS graph (k=10, p=0.1, seed 2), ordered
                        neighbours, float32 opinion + float32[8] weights, 50 ticks
 """
@@ -394,6 +401,110 @@ def helpers_er():
                         history=hist, visits=visits)
 
 
+def fraction_er():
+    from ref_steps import fraction_step
+    from sagesim.breed import Breed
+    from sagesim.model import Model
+    from sagesim.space import NetworkSpace
+
+    from sagesim_gb300 import graphs
+
+    off, idx = graphs.erdos_renyi(1500, 0.004, 13)
+    n = off.size - 1
+    rng = np.random.default_rng(13)
+    st = np.ones(n, dtype=np.int32)
+    st[rng.choice(n, 30, replace=False)] = 2
+    load0 = rng.integers(0, 4, size=n).astype(np.int32)
+    model = Model(NetworkSpace(), step_function_file_path="step_func_code_gold_frac.py")
+    br = Breed("SIR")
+    br.register_property("state", 1)
+    br.register_property("immunity", 0)
+    br.register_property("load", 0)
+    br.register_step_func(fraction_step, os.path.join(HERE, "ref_steps.py"), priority=0)
+    model.register_breed(br)
+    model.register_global_property("p_infection", 0.4)
+    model.register_global_property("p_recovery", 0.1)
+    model.set_seed(13)
+    for i in range(n):
+        model.create_agent_of_breed(br, state=int(st[i]), load=int(load0[i]))
+    sp = model.get_space()
+    for i in range(n):
+        for k in range(off[i], off[i + 1]):
+            sp.connect_agents(i, int(idx[k]), directed=True)
+    model._max_blocks_per_sm = 1
+    model.setup(use_gpu=True)
+    keep = [1, 2, 5, 10, 25]
+    states, imm, load = [], [], []
+    for t in range(1, keep[-1] + 1):
+        model.simulate(1, sync_workers_every_n_ticks=1)
+        if t in keep:
+            states.append(states_by_agent(model, "state").astype(np.int8))
+            imm.append(states_by_agent(model, "immunity").astype(np.float32))
+            load.append(states_by_agent(model, "load").astype(np.float32))
+    clear_generated()
+    np.savez_compressed(os.path.join(HERE, "fraction_er.npz"), offsets=off, indices=idx, state0=st.astype(np.int8),
+                        load0=load0, ticks=np.array(keep), state=np.stack(states), immunity=np.stack(imm),
+                        load=np.stack(load))
+
+
+def binding_model(cls, codefile):
+    """The SIR model of the binding fixture, built through the reference's own
+    API as a SAGESim user would (connect_agents on a set-based space)."""
+    import test_simulation as ts
+    from sagesim.breed import Breed
+
+    from sagesim_gb300 import graphs
+
+    off, idx = graphs.erdos_renyi(2000, 0.004, 17)
+    n = off.size - 1
+    rng = np.random.default_rng(17)
+    st = np.ones(n, dtype=np.int32)
+    st[rng.choice(n, 20, replace=False)] = 2
+    from sagesim.space import NetworkSpace
+
+    model = cls(NetworkSpace(), step_function_file_path=codefile)
+    br = Breed("SIR")
+    br.register_property("state", 1)
+    br.register_step_func(ts.sir_step_func, ts.__file__, priority=0)
+    model.register_breed(br)
+    model.register_global_property("p_infection", 0.3)
+    model.register_global_property("p_recovery", 0.1)
+    model.set_seed(17)
+    for i in range(n):
+        model.create_agent_of_breed(br, state=int(st[i]))
+    sp = model.get_space()
+    for i in range(n):
+        for k in range(off[i], off[i + 1]):
+            if idx[k] > i:
+                sp.connect_agents(i, int(idx[k]))
+    for a in rng.choice(n, 100, replace=False):
+        model.set_agent_logical_id(int(a), int(rng.integers(0, 2**24)))
+    return model
+
+
+def integration_binding_namespace():
+    """Executes the two binding blocks of INTEGRATION.md (the engine side and the
+    SAGESim side) in one namespace."""
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    ns = {}
+    for tag in ("engine", "sagesim"):
+        body = text.split("<!-- binding:%s -->" % tag, 1)[1].split("```python", 1)[1].split("```", 1)[0]
+        exec(compile(body, "INTEGRATION.md:binding:" + tag, "exec"), ns)
+    return ns
+
+
+def binding_er():
+    from sagesim.model import Model
+
+    ns = integration_binding_namespace()
+    x = binding_model(ns["GB300SIRModel"], "step_func_code_gold_bind0.py").gb300_inputs()
+    clear_generated()
+    hist = run_ticks(binding_model(Model, "step_func_code_gold_bind1.py"), "state", 30, np.int8)
+    clear_generated()
+    np.savez_compressed(os.path.join(HERE, "binding_er.npz"), history=hist,
+                        **{"in_" + k: np.asarray(v) for k, v in x.items()})
+
+
 def main():
     reference = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SAGESIM_REFERENCE", "")
     if not reference or not os.path.isdir(os.path.join(reference, "sagesim")):
@@ -402,9 +513,10 @@ def main():
     work = tempfile.mkdtemp(prefix="sg_golden_")
     os.chdir(work)  # the reference writes its generated step module into the CWD
     which = sys.argv[2:] or ["philox", "chain", "hier", "db", "er", "breeds", "bla", "measures", "helpers",
-                             "opinion"]
+                             "fraction", "binding", "opinion"]
     jobs = {"philox": philox_vectors, "chain": chains, "hier": hierarchy, "db": db_priority,
             "er": er_c1, "breeds": ba_breeds, "bla": bla_two_breeds, "measures": measures_er, "helpers": helpers_er,
+            "fraction": fraction_er, "binding": binding_er,
             "opinion": opinion_ws}
     for w in which:
         print("generating", w, flush=True)

@@ -27,6 +27,11 @@ measures_step: SIR with per-agent protective measures (a float32[4] list
 helpers_step: per-neighbour SIR written with the device helpers of
   sagesim/utils.py (get_num_neighbors / get_neighbor on the CSR names,
   get_ / set_this_agent_data_from_tensor) plus a float32 visit counter.
+fraction_step: SIR whose two extra properties start as whole numbers (an int
+  default and int initial values) and are written fractions: a susceptible
+  agent with infected neighbours gains 0.25 immunity per tick (up to 1) and is
+  infected when philox(salt 1) < p_infection * (1 - immunity); every agent's
+  load becomes (load + infected neighbours) / 2.
 opinion_step: weighted mean of the first min(deg, 8) ordered neighbours'
   opinions (float32 arithmetic in row order, normalised by the sum of |w|),
   plus noise_sigma * rand_normal(salt 1) in float64, clamped to [0, 1].
@@ -221,3 +226,28 @@ def helpers_step(
                 j += 1
             i += 1
     visits[agent_index] = visits[agent_index] + 1
+
+
+@jit.rawkernel(device="cuda")
+def fraction_step(
+    tick, agent_index, p_infection, p_recovery,
+    agent_ids, breeds, locations, state_tensor, immunity, load,
+):
+    neighbor_ids = locations[agent_index]
+    agent_state = int(state_tensor[agent_index])
+    infected = 0
+    i = 0
+    while i < len(neighbor_ids) and neighbor_ids[i] != -1:
+        if int(state_tensor[neighbor_ids[i]]) == 2:
+            infected += 1
+        i += 1
+    load[agent_index] = (load[agent_index] + infected) / 2
+    if agent_state == 2:
+        if rand_uniform_philox(tick, agent_index, 1) < p_recovery:
+            state_tensor[agent_index] = 3
+    elif agent_state == 1:
+        if infected > 0:
+            if rand_uniform_philox(tick, agent_index, 1) < p_infection * (1.0 - immunity[agent_index]):
+                state_tensor[agent_index] = 2
+            if immunity[agent_index] < 1.0:
+                immunity[agent_index] = immunity[agent_index] + 0.25

@@ -295,3 +295,47 @@ def test_model_pickles_without_an_engine():
     assert m2.get_space().get_location(3) == [0]
     assert m2.get_agent_property_value(2, "state") == 2 and m2.get_agent_property_value(1, "w") == [1, -1]
     assert m2._breed_local_arrays[0]["shape_per_agent"] == (2,)
+
+
+def test_property_types_follow_what_steps_write():
+    """Whole-number properties stay int32 only when no Python-dialect step
+    writes them (or a builtin SIR step, whose state is int32, does); a property
+    a translated step writes is float32 as in the reference, so a stored
+    fraction is kept; values outside int32 are float32."""
+    here = Path(__file__).resolve().parent / "golden" / "ref_steps.py"
+
+    class Ref:
+        __name__ = "fraction_step"
+
+    m = Model(NetworkSpace())
+    br = Breed("SIR")
+    br.register_property("state", 1)
+    br.register_property("immunity", 0)
+    br.register_property("load", 0)
+    br.register_property("tag", 7)
+    br.register_property("big", 0)
+    br.register_step_func(Ref(), str(here), 0)
+    m.register_breed(br)
+    m.register_global_property("p_infection", 0.4)
+    m.register_global_property("p_recovery", 0.1)
+    for i in range(5):
+        m.create_agent_of_breed(br, state=1, load=i, big=2**33 if i == 3 else 0)
+    m._collect_steps()
+    m._build_host_arrays()
+    types = {k: v[0] for k, v in m._props.items()}
+    assert types["immunity"] == np.float32 and types["load"] == np.float32 and types["state"] == np.float32
+    assert types["tag"] == np.int32  # read by no step, written by none
+    assert types["big"] == np.float32  # beyond int32
+
+    m2 = Model(NetworkSpace())
+    b2 = Breed("SIR")
+    b2.register_property("state", 1)
+    b2.register_step_func(SIRStep("B"), None, 0)
+    m2.register_breed(b2)
+    m2.register_global_property("p_infection", 0.4)
+    m2.register_global_property("p_recovery", 0.1)
+    for i in range(3):
+        m2.create_agent_of_breed(b2, state=1)
+    m2._collect_steps()
+    m2._build_host_arrays()
+    assert m2._props["state"][0] == np.int32  # the builtin SIR step needs int32 state

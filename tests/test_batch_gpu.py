@@ -128,3 +128,32 @@ def test_batch_errors():
         b.commit()
         with pytest.raises(SageSimError):
             b.add_scenario(variant="B", **sc)
+
+
+def test_ensemble_members_up_to_a_million_agents_match_oracle():
+    """Members of the 512-scenario ensemble's size range, the largest at 10^6
+    agents, advanced together for its 365 ticks with the default tuned launch
+    configuration: each equals the oracle (SIR-B, own seed and parameters)."""
+    specs = [("ba", 1_000_000, 5, 31), ("ws", 600_000, 10, 0.1, 32), ("er", 400_000, 8.0 / 399_999, 33),
+             ("ba", 3_000, 3, 34), ("er", 1_000, 8.0 / 999, 35)]
+    rng = np.random.default_rng(36)
+    scs = []
+    for spec in specs:
+        off, idx = graphs.generate(spec)
+        n = off.size - 1
+        st = np.ones(n, dtype=np.int32)
+        st[rng.choice(n, max(1, int(0.005 * n)), replace=False)] = 2
+        scs.append(dict(offsets=off, indices=idx, state=st, seed=int(rng.integers(0, 2**31)),
+                        beta=float(rng.uniform(0.01, 0.1)), gamma=float(rng.uniform(0.05, 0.2)), horizon=365))
+    with Batch() as b:
+        sids = [b.add_scenario(variant="B", **sc) for sc in scs]
+        b.commit()
+        b.snapshot()
+        b.tune(2)
+        b.restore()
+        b.run(365)
+        b.synchronize()
+        for sid, sc in zip(sids, scs):
+            ref, _, _ = oracle.sir_run(2, sc["offsets"], sc["indices"], sc["state"], sc["seed"], 0, 365,
+                                       sc["beta"], sc["gamma"])
+            assert np.array_equal(b.get_state(sid), ref), sid

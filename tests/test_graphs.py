@@ -78,3 +78,17 @@ def test_bad_permutation_rejected():
     idx = np.array([1, 0], dtype=np.int32)
     with pytest.raises(SageSimError):
         graphs.permute_csr(off, idx, np.array([0, 0], dtype=np.int32))
+
+
+@pytest.mark.parametrize("n,m,seed", [(3, 4, 0), (5, 4, 1), (1000, 3, 7), (200_000, 4, 1), (50_000, 6, 2**63 + 5)])
+def test_oracle_barabasi_albert_equals_the_engine_generator(n, m, seed):
+    """The CPU baseline builds the benchmark's graph with oracle/'s own
+    generator (no engine library in that process); both follow the same
+    definition and must give the same CSR, row order included."""
+    from oracle import oracle
+
+    a_off, a_idx = oracle.barabasi_albert(n, m, seed)
+    b_off, b_idx = graphs.barabasi_albert(n, m, seed)
+    assert np.array_equal(a_off, b_off) and np.array_equal(a_idx, b_idx)
+    assert np.array_equal(oracle.initial_infected(n, 0.01, seed % 2**32),
+                          graphs.initial_infected(n, 0.01, seed % 2**32))

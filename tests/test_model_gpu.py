@@ -568,3 +568,33 @@ def fmod_step(tick, agent_index, d, agent_ids, breeds, locations, x, y):
     m.simulate(1)
     want = np.remainder(x.astype(np.float64), -2.5).astype(np.float32)
     assert np.array_equal(m.get_property_array("y"), want)
+
+
+def test_python_dialect_step_writes_fractions_into_whole_number_properties():
+    """Two properties start as whole numbers (an int default, int initial
+    values) and a reference-dialect step stores fractions into them (immunity
+    += 0.25, load = (load + k) / 2). The reference keeps both in float32; here
+    they must not be truncated: states, immunity and load equal the reference
+    pipeline's (fraction_er.npz) after ticks 1, 2, 5, 10, 25."""
+    d = gold("fraction_er.npz")
+    off, idx = d["offsets"], d["indices"]
+    n = off.size - 1
+    m = Model(NetworkSpace())
+    br = Breed("SIR")
+    br.register_property("state", 1)
+    br.register_property("immunity", 0)
+    br.register_property("load", 0)
+    br.register_step_func(_PyStepRef("fraction_step"), REF_STEPS, 0)
+    m.register_breed(br)
+    m.register_global_property("p_infection", 0.4)
+    m.register_global_property("p_recovery", 0.1)
+    m.set_seed(13)
+    m.create_agents_bulk(br, n, state=d["state0"].astype(np.int32), load=d["load0"])
+    m.get_space().set_csr(off, idx)
+    m.setup()
+    for j, t in enumerate(d["ticks"]):
+        m.simulate(int(t) - m.tick)
+        assert np.array_equal(m.get_property_array("state"), d["state"][j]), "state, tick %d" % t
+        assert np.array_equal(m.get_property_array("immunity"), d["immunity"][j]), "immunity, tick %d" % t
+        assert np.array_equal(m.get_property_array("load"), d["load"][j]), "load, tick %d" % t
+    assert (d["immunity"][-1] % 1 != 0).any() and (d["load"][-1] % 1 != 0).any()

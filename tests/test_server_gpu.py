@@ -96,3 +96,44 @@ def test_bad_csr_is_refused_on_both_submission_paths():
             while srv.poll(rid)[0] != 2:
                 srv.step(16)
             assert np.array_equal(srv.take_result(rid), standalone(other, "B", other["horizon"]))
+
+
+def test_requests_with_logical_ids_alone_and_in_the_mix():
+    """Requests relabelled for locality carry logical ids (the original agent
+    ids, the key of every draw as in sagesim/model.py:656-667): served in a mix
+    with plain requests, each result equals its standalone run, and mapped back
+    through the relabelling it equals the oracle's run of the graph in its
+    original order."""
+    from oracle import oracle
+    from sagesim_gb300 import graphs
+
+    base = requests(12, 15)
+    reqs, perms, originals = [], [], []
+    for k, r in enumerate(base):
+        if k % 2:
+            off, idx = r["offsets"], r["indices"]
+            n = off.size - 1
+            perm, _ = graphs.partition_relabel(off, idx, 8, k)
+            roff, ridx = graphs.permute_csr(off, idx, perm)
+            rst = np.empty_like(r["state"])
+            rst[perm] = r["state"]
+            lids = np.empty(n, dtype=np.int64)
+            lids[perm] = np.arange(n, dtype=np.int64)
+            reqs.append(dict(r, offsets=roff, indices=ridx, state=rst, lids=lids))
+            perms.append(perm)
+        else:
+            reqs.append(dict(r))
+            perms.append(None)
+        originals.append(r)
+    sizes = [r["offsets"].size - 1 for r in reqs]
+    budget = int(sum(sorted(sizes)[-5:]) * 64)  # a few resident at once: some requests queue
+    arrivals = np.cumsum(np.random.default_rng(5).exponential(0.004, size=len(reqs)))
+    with Server(budget_bytes=budget, agent_slots=2_000_000, edge_slots=40_000_000, variant="B") as srv:
+        out = serve_stream(srv, reqs, arrivals, chunk=8)
+    for i, r in enumerate(reqs):
+        assert np.array_equal(out["results"][i], standalone(r, "B", r["horizon"])), "request %d" % i
+        o = originals[i]
+        want, _, _ = oracle.sir_run(2, o["offsets"], o["indices"], o["state"], o["seed"], 0, o["horizon"],
+                                    o["beta"], o["gamma"])
+        got = out["results"][i] if perms[i] is None else out["results"][i][perms[i]]
+        assert np.array_equal(got, want), "request %d against the oracle" % i

@@ -7,15 +7,17 @@ the state back in place; every piece of scratch memory comes from a static
 device array inside the library. This test allocates the inputs and outputs
 itself (through torch, as such a caller would with its own allocator), calls
 the entry point through the C ABI twice in a row on different graphs, and
-checks each result against the regular engine entry point (bit-exact, the
-tolerance every integer-state test here uses). It lives in a file collected
-last so that a run stopping at the first failure has run every other test.
+checks each result against the regular engine entry point and against the
+oracle (bit-exact, the tolerance every integer-state test here uses), also at
+the entry point's largest agent count. It lives in a file collected last so
+that a run stopping at the first failure has run every other test.
 """
 import ctypes
 
 import numpy as np
 import pytest
 
+from oracle import oracle
 from sagesim_gb300 import Engine, _native, graphs
 
 pytestmark = pytest.mark.gpu
@@ -60,6 +62,8 @@ def test_noalloc_matches_engine_on_two_calls_in_a_row():
     want1 = _reference_run(off1, idx1, st1, _native.SG_BUILTIN_SIR_B, 5, 0, 40, 0.05, 0.1)
     got1 = _noalloc_run(lib, torch, off1, idx1, st1, _native.SG_BUILTIN_SIR_B, 5, 0, 40, 0.05, 0.1)
     assert np.array_equal(got1, want1)
+    # the oracle (draws keyed on the agent index, as the entry point keys them)
+    assert np.array_equal(got1, oracle.sir_run(2, off1, idx1, st1, 5, 0, 40, 0.05, 0.1)[0])
     # second call right after, smaller ER graph (the scratch array still holds
     # the first call's counts and change lists), SIR-A, ticks 7..36
     off2, idx2 = graphs.erdos_renyi(150_000, 8.0 / 150_000, 22)
@@ -67,7 +71,27 @@ def test_noalloc_matches_engine_on_two_calls_in_a_row():
     want2 = _reference_run(off2, idx2, st2, _native.SG_BUILTIN_SIR_A, 9, 7, 30, 0.2, 0.1)
     got2 = _noalloc_run(lib, torch, off2, idx2, st2, _native.SG_BUILTIN_SIR_A, 9, 7, 30, 0.2, 0.1)
     assert np.array_equal(got2, want2)
+    assert np.array_equal(got2, oracle.sir_run(1, off2, idx2, st2, 9, 7, 30, 0.2, 0.1)[0])
     assert not np.array_equal(got2, st2)  # the epidemic moved
+
+
+def test_noalloc_at_the_size_limit():
+    """n == SG_NOALLOC_MAX_AGENTS exactly: every part of the scratch array
+    (counts, change lists, tile counters, tile table, segment record) is used
+    up to its last entry, twice in a row."""
+    torch = pytest.importorskip("torch")
+    lib = _native.load()
+    n = 1048576  # SG_NOALLOC_MAX_AGENTS
+    off, idx = graphs.erdos_renyi(n, 10.0 / n, 23)
+    assert off.size - 1 == n
+    st = _state(n, 0.002, 23)
+    for tick0, nticks in ((0, 12), (12, 6)):
+        want = _reference_run(off, idx, st, _native.SG_BUILTIN_SIR_B, 3, tick0, nticks, 0.08, 0.05)
+        got = _noalloc_run(lib, torch, off, idx, st, _native.SG_BUILTIN_SIR_B, 3, tick0, nticks, 0.08, 0.05)
+        assert np.array_equal(got, want)
+        assert np.array_equal(got, oracle.sir_run(2, off, idx, st, 3, tick0, nticks, 0.08, 0.05)[0])
+        assert not np.array_equal(got, st)
+        st = got
 
 
 def test_noalloc_rejects_sizes_beyond_the_limit():
