@@ -136,7 +136,7 @@ typedef struct sg_tune {
     int32_t blocks_per_sm;     /* persistent grid = blocks_per_sm x SM count     */
     int32_t thread_row;        /* rows up to this length: one lane; longer: warp */
     int32_t mega_row;          /* rows longer than this: a whole block           */
-    int32_t count_flavour;     /* count strategy, bit mask (0..31):              */
+    int32_t count_flavour;     /* count strategy, bit mask (0..1023):            */
                                /*  1 = 8 agents per thread (else 4)              */
                                /*  2 = warp-dense SIR-B draws                    */
                                /*  4 = count and RNG key loaded only where needed*/
@@ -149,8 +149,14 @@ typedef struct sg_tune {
                                /* 256 = with 16: hybrid, the loop form of bits   */
                                /*      0-2 in busy ticks (decided on the GPU;    */
                                /*      graphs of 24+ tiles per SM, or with 32)   */
-                               /* default 278: class sweep + hybrid whose loop   */
-                               /*      form has warp-dense draws and lazy loads  */
+                               /* 512 = flat draws in place of the loop form     */
+                               /*      (in-place runs): a block lays its tile's  */
+                               /*      draws end to end, each thread an equal    */
+                               /*      share                                     */
+                               /* default 790: class sweep + hybrid whose busy-  */
+                               /*      tick form is the flat draws (the loop     */
+                               /*      form's bits 2 and 4 apply where flat      */
+                               /*      draws cannot run: runs not in place)      */
     double us_per_tick;        /* measured by sg_batch_tune (output)             */
 } sg_tune;
 
@@ -263,6 +269,13 @@ int sg_profile_enable(sg_engine *e, int32_t on);
 int sg_profile_get(sg_engine *e, int32_t kind, char *name, size_t cap, int64_t *launches,
                    double *total_ms);
 
+/* The opinion step's cosine cos(2 pi k / 2^23) (the Box-Muller angle of
+ * sagesim/math_utils.py:250-255) as the step forms it from its split tables,
+ * split[q], and evaluated directly with the device's cos, direct[q], for
+ * k = k0 .. k0 + n - 1 (k0 + n <= 2^23). A check of the engine's own table
+ * method; no counterpart in the reference. */
+int sg_opinion_cosine_check(sg_engine *e, int32_t k0, int32_t n, double *split, double *direct);
+
 /* ---- ensembles: many independent SIR scenarios in one launch per tick ---------------
  * No single counterpart in the reference, which runs one model per process
  * (sagesim/model.py:961-998); each scenario here is what one reference Model
@@ -340,6 +353,15 @@ typedef struct sg_server_cfg {
 #define SG_REQ_QUEUED 0
 #define SG_REQ_RUNNING 1
 #define SG_REQ_DONE 2
+/* A borrowed request whose CSR the device check refused when it was placed;
+ * sg_server_take_result then returns SG_ERR_BAD_CSR and forgets it. */
+#define SG_REQ_FAILED 3
+/* sg_scenario_desc.flags for sg_server_submit: the caller keeps offsets,
+ * indices, state and lids valid and unchanged until the request has left the
+ * queue (poll status other than SG_REQ_QUEUED). A queued request then keeps
+ * the pointers instead of host copies, and its CSR is checked on the device
+ * when it is placed (no host pass over the edges at submission). */
+#define SG_REQ_BORROW 256
 
 int sg_server_create(const sg_server_cfg *cfg, sg_server **out);
 int sg_server_destroy(sg_server *s);

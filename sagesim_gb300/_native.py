@@ -38,6 +38,8 @@ SG_SIR_FRONTIER = 2
 SG_REQ_QUEUED = 0
 SG_REQ_RUNNING = 1
 SG_REQ_DONE = 2
+SG_REQ_FAILED = 3
+SG_REQ_BORROW = 256
 
 SG_GRAPH_ORDERED = 1
 SG_GRAPH_SYMMETRIC = 2
@@ -132,6 +134,7 @@ SIGNATURES = {
     "sg_restore": [_P],
     "sg_profile_enable": [_P, _I32],
     "sg_profile_get": [_P, _I32, ctypes.c_char_p, _SZ, ctypes.POINTER(_I64), ctypes.POINTER(_D)],
+    "sg_opinion_cosine_check": [_P, _I32, _I32, _P, _P],
     "sg_batch_create": [ctypes.POINTER(EngineCfg), ctypes.POINTER(_P)],
     "sg_batch_destroy": [_P],
     "sg_batch_last_error": [_P, ctypes.c_char_p, _SZ],

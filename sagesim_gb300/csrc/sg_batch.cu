@@ -27,8 +27,8 @@ namespace {
 constexpr int32_t kLongRowFloor = 512; // rows kept as mega candidates (smallest tunable mega_row)
 // count-step flavours the autotuner times: loop form (4 or 8 agents per thread,
 // eager or lazy loads, per-lane or warp-dense draws) and class sweep with the
-// load-balanced scatter (alone or in the hybrid), and two of them with the
-// lane-per-row scatter
+// load-balanced scatter (alone or in the hybrid), two of them with the
+// lane-per-row scatter, and flat draws (every tick, or the hybrid's busy ticks)
 constexpr int32_t kCountFlavourCands[] = {0,
                                           1,
                                           4,
@@ -41,7 +41,10 @@ constexpr int32_t kCountFlavourCands[] = {0,
                                           SG_FLAVOUR_SWEEP | SG_FLAVOUR_HYBRID,
                                           SG_FLAVOUR_SWEEP | SG_FLAVOUR_FORCE | SG_FLAVOUR_HYBRID,
                                           SG_FLAVOUR_ROWSCATTER | 4,
-                                          SG_FLAVOUR_ROWSCATTER | SG_FLAVOUR_SWEEP};
+                                          SG_FLAVOUR_ROWSCATTER | SG_FLAVOUR_SWEEP,
+                                          SG_FLAVOUR_FLAT | 4,
+                                          SG_FLAVOUR_SWEEP | SG_FLAVOUR_HYBRID | SG_FLAVOUR_FLAT | SG_FLAVOUR_DENSE |
+                                              SG_FLAVOUR_LAZY};
 }
 
 int64_t SgRanges::take(int64_t len)
@@ -148,6 +151,15 @@ int SgPool::upload(void *dst, const void *src, size_t bytes)
     if (bytes < kStageMin) {
         POOL_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream));
         return SG_OK;
+    }
+    {
+        // page-locked source (e.g. a server's receive buffers): one direct copy
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, src) == cudaSuccess && at.type == cudaMemoryTypeHost) {
+            POOL_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream));
+            return SG_OK;
+        }
+        (void)cudaGetLastError();
     }
     if (!stage[0]) {
         for (int h = 0; h < 2; ++h) {

@@ -84,7 +84,7 @@ struct sg_engine {
     bool last_sweep = false; // the last run's count step was the class sweep
     SgDev flist[2], flen, fnch, fmark, fstats_init, fstats_delta; // frontier strategy
     SgDev transpose_tmp, scan_tmp;
-    SgDev bm_radius, bm_cos; // opinion: Box-Muller tables, built once per engine
+    SgDev bm_radius, bm_trig; // opinion: Box-Muller tables, built once per engine
     bool bm_ready = false;
     bool l2_limit_set = false;
     SgDev prop_table; // sg_prop_dev per property, for compiled steps
@@ -92,7 +92,7 @@ struct sg_engine {
     SgProfiler prof;
     int hub_deg = 32;
     sg_tune tune{SG_SIR_COUNT, 16, 32, 2048,
-                 SG_FLAVOUR_SWEEP | SG_FLAVOUR_HYBRID | SG_FLAVOUR_DENSE | SG_FLAVOUR_LAZY, 0.0};
+                 SG_FLAVOUR_SWEEP | SG_FLAVOUR_HYBRID | SG_FLAVOUR_FLAT | SG_FLAVOUR_DENSE | SG_FLAVOUR_LAZY, 0.0};
     int32_t last_nticks = 0;
     int64_t last_launches = 0; // kernels launched by the last enqueued run
     std::vector<int64_t> hist;  // per-tick S, I, R, E_S of consecutive runs with statistics
@@ -789,11 +789,16 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
                                    sg_launch_sir_pull(a, variant, stats_on, grid + a.mega_blocks, e->stream));
                 }
             } else if (s->kind == SG_BUILTIN_OPINION) {
-                a.bm_radius = e->bm_ready ? e->bm_radius.as<double>() : nullptr;
-                a.bm_cos = e->bm_ready ? e->bm_cos.as<double>() : nullptr;
+                a.bm_radius = e->bm_ready ? e->bm_radius.as<float2>() : nullptr;
+                a.bm_trig = e->bm_ready ? e->bm_trig.as<float2>() : nullptr;
+                {
+                    const double sg = s->bp.sigma;
+                    a.sigma_hi = (float)sg;
+                    a.sigma_lo = (float)(sg - (double)a.sigma_hi);
+                }
                 if (e->bm_ready && e->l2_limit_bytes) {
-                    a.l2_win = a.bm_cos;
-                    a.l2_win_bytes = std::min(e->l2_window_max, (size_t)SG_BOX_MULLER_SIZE * sizeof(double));
+                    a.l2_win = a.bm_radius;
+                    a.l2_win_bytes = std::min(e->l2_window_max, (size_t)SG_BOX_MULLER_SIZE * sizeof(float2));
                     a.l2_win_hit = (float)std::min(1.0, (double)e->l2_limit_bytes / (double)a.l2_win_bytes);
                 }
                 SG_PROF_LAUNCH("opinion", sg_launch_opinion(a, grid, e->stream, s->host_seg.width));
@@ -881,9 +886,9 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
         rc = prepare_step(e, s, tick0, stats);
         if (rc) return rc;
         if (s->kind == SG_BUILTIN_OPINION && !e->bm_ready) { // before any capture
-            SG_CK(e->bm_radius.reserve((size_t)SG_BOX_MULLER_SIZE * sizeof(double)));
-            SG_CK(e->bm_cos.reserve((size_t)SG_BOX_MULLER_SIZE * sizeof(double)));
-            SG_CK(sg_launch_opinion_tables(e->bm_radius.as<double>(), e->bm_cos.as<double>(), e->stream));
+            SG_CK(e->bm_radius.reserve((size_t)SG_BOX_MULLER_SIZE * sizeof(float2)));
+            SG_CK(e->bm_trig.reserve((size_t)SG_BM_TRIG_ENTRIES * sizeof(float2)));
+            SG_CK(sg_launch_opinion_tables(e->bm_radius.as<float2>(), e->bm_trig.as<float2>(), e->stream));
             e->bm_ready = true;
         }
     }
@@ -913,8 +918,8 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
         e->l2_limit_set = true;
     }
     if (e->bm_ready && e->l2_window_max && !e->l2_limit_set) {
-        // the opinion step's cosine table (64 MiB, read at random) as persisting lines
-        e->l2_limit_bytes = std::min(e->l2_window_max, (size_t)SG_BOX_MULLER_SIZE * sizeof(double));
+        // the opinion step's radius table (64 MiB, read at random) as persisting lines
+        e->l2_limit_bytes = std::min(e->l2_window_max, (size_t)SG_BOX_MULLER_SIZE * sizeof(float2));
         cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, e->l2_limit_bytes);
         (void)cudaGetLastError();
         e->l2_limit_set = true;
@@ -1159,6 +1164,27 @@ int sg_profile_get(sg_engine *e, int32_t kind, char *name, size_t cap, int64_t *
     }
     if (launches) *launches = k.launches;
     if (total_ms) *total_ms = k.total_ms;
+    return SG_OK;
+}
+
+int sg_opinion_cosine_check(sg_engine *e, int32_t k0, int32_t n, double *split, double *direct)
+{
+    if (!e || k0 < 0 || n < 0 || (int64_t)k0 + n > SG_BOX_MULLER_SIZE || (n > 0 && (!split || !direct)))
+        return SG_ERR_INVALID;
+    if (n == 0) return SG_OK;
+    cudaSetDevice(e->device);
+    SgDev trig, out;
+    SG_CK(trig.reserve((size_t)SG_BM_TRIG_ENTRIES * sizeof(float2)));
+    SG_CK(out.reserve((size_t)n * 2 * sizeof(double)));
+    SG_CK(sg_launch_opinion_tables(nullptr, trig.as<float2>(), e->stream));
+    SG_CK(sg_launch_opinion_cos_check(trig.as<float2>(), k0, n, out.as<double>(), e->stream));
+    std::vector<double> h((size_t)n * 2);
+    SG_CK(cudaMemcpyAsync(h.data(), out.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    SG_CK(cudaStreamSynchronize(e->stream));
+    for (int32_t q = 0; q < n; ++q) {
+        split[q] = h[2 * (size_t)q];
+        direct[q] = h[2 * (size_t)q + 1];
+    }
     return SG_OK;
 }
 

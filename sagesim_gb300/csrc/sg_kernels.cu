@@ -14,6 +14,8 @@
 // kernels are in sg_count.cu.
 #include <cub/device/device_scan.cuh>
 
+#include <mutex>
+
 #include "sg_device.cuh"
 
 namespace {
@@ -371,14 +373,30 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) frontier_scatter_kernel(SgTick
 // over the first min(deg, width) ordered neighbours; float32 sums in row order
 // with every multiply and add rounded (no FMA), Box-Muller in double
 // (sagesim/math_utils.py:231-255: u1 salt 1, u2 salt 1 + 73856093, +1e-10
-// guard). u1 and u2 are k / 2^23 for 23-bit Philox integers k, so
-// sqrt(-2 log(u1 + 1e-10)) and cos(2 pi u2) take 2^23 values each: they are
-// tabulated once (opinion_tables_kernel, the same double expressions) and an
-// agent's normal is two table reads and one multiply, bit for bit the same as
-// evaluating it -- the double-precision transcendentals otherwise cost ten
-// times the tick's memory traffic. (A float32 Box-Muller was tried and
-// rejected: opinions near the clamp at 0 differ by up to 1.5e-4 relative.)
+// guard). u1 and u2 are k / 2^23 for 23-bit Philox integers k.
+//  - radius sqrt(-2 log(u1 + 1e-10)) takes 2^23 values: it is evaluated once
+//    per engine in double (opinion_tables_kernel) and tabulated (64 MiB, kept
+//    in L2 as persisting lines);
+//  - cos(2 pi u2) by the angle-addition formula cos(A + B) = cos A cos B -
+//    sin A sin B with k = 2048 kh + kl, A = 2 pi kh / 2^12, B = 2 pi kl / 2^23:
+//    cos A from a 4096-entry table (sin A is the same table a quarter turn
+//    back), cos B and sin B from 2048-entry tables (built with sincospi and
+//    copied into shared memory by every block);
+//  - every table entry is a double-float pair (hi, lo) of float32 whose sum is
+//    the double value to about 2^-48 relative, and the noise term
+//    sigma * radius * cosine and its sum with the float32 mean are formed in
+//    double-float arithmetic on the FP32 units (Dekker's exact product via
+//    fused multiply-add and Knuth's two-sum). This GPU's FP64 units run at a
+//    small fraction of its FP32 rate; with double arithmetic they bounded the
+//    tick. The result rounds to the same float32 as the reference's double
+//    expression except within about 2^-46 of a float32 rounding boundary
+//    (one float32 ulp apart there); the tests compare with the oracle at 1e-6
+//    relative and check the cosine against the device's own cos.
+// (A float32 Box-Muller was tried and rejected: opinions near the clamp at 0
+// differ by up to 1.5e-4 relative.)
 constexpr int32_t kBoxMullerSize = 1 << 23;
+constexpr int32_t kTrigA = 4096, kTrigB = 2048; // entries of the A (cos) and B (cos, sin) tables
+static_assert(kTrigA + 2 * kTrigB == SG_BM_TRIG_ENTRIES, "table layout");
 
 __device__ __forceinline__ double bm_radius(uint32_t k)
 {
@@ -392,13 +410,91 @@ __device__ __forceinline__ double bm_cos(uint32_t k)
     return cos(__dmul_rn(6.283185307179586, u2));
 }
 
-__global__ void opinion_tables_kernel(double *__restrict__ radius, double *__restrict__ cosine)
+// ---- double-float arithmetic (hi + lo, |lo| <= ulp(hi) / 2) ----
+__device__ __forceinline__ float2 ff_split(double v)
 {
-    for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < kBoxMullerSize; k += gridDim.x * blockDim.x) {
-        radius[k] = bm_radius((uint32_t)k);
-        cosine[k] = bm_cos((uint32_t)k);
+    const float hi = __double2float_rn(v);
+    return make_float2(hi, __double2float_rn(v - (double)hi));
+}
+
+// a + b exactly as s + e (Knuth's two-sum; any magnitudes)
+__device__ __forceinline__ float2 ff_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return make_float2(s, e);
+}
+
+// s + e renormalised when |s| >= |e| (fast two-sum)
+__device__ __forceinline__ float2 ff_norm(float s, float e)
+{
+    const float h = __fadd_rn(s, e);
+    return make_float2(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+
+// a * b: exact product of the high parts (Dekker, via fma) plus the cross terms
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b)
+{
+    const float p = __fmul_rn(a.x, b.x);
+    float e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, e);
+    e = __fmaf_rn(a.y, b.x, e);
+    return ff_norm(p, e);
+}
+
+// a + b
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b)
+{
+    float2 s = ff_two_sum(a.x, b.x);
+    const float2 t = ff_two_sum(a.y, b.y);
+    s = ff_norm(s.x, __fadd_rn(s.y, t.x));
+    return ff_norm(s.x, __fadd_rn(s.y, t.y));
+}
+
+// trig = [cos A (4096)][cos B (2048)][sin B (2048)] as double-float pairs, in
+// global or shared memory
+__device__ __forceinline__ float2 bm_cos_split(const float2 *trig, uint32_t k)
+{
+    const uint32_t kh = k >> 11, kl = k & (kTrigB - 1);
+    const float2 ca = trig[kh], sa = trig[(kh - kTrigA / 4) & (kTrigA - 1)]; // sin A = cos(A - pi/2)
+    const float2 cb = trig[kTrigA + kl], sb = trig[kTrigA + kTrigB + kl];
+    const float2 p = ff_mul(sa, sb);
+    return ff_add(ff_mul(ca, cb), make_float2(-p.x, -p.y));
+}
+
+__global__ void opinion_tables_kernel(float2 *__restrict__ radius, float2 *__restrict__ trig)
+{
+    const int32_t stride = gridDim.x * blockDim.x;
+    const int32_t end = radius ? kBoxMullerSize : kTrigA; // radius NULL: the cosine tables only
+    for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < end; k += stride) {
+        if (radius) radius[k] = ff_split(bm_radius((uint32_t)k));
+        if (k < kTrigA) { // A = pi * k / 2^11
+            double sv, cv;
+            sincospi((double)k / 2048.0, &sv, &cv);
+            trig[k] = ff_split(cv);
+        }
+        if (k < kTrigB) { // B = pi * k / 2^22
+            double sv, cv;
+            sincospi((double)k / 4194304.0, &sv, &cv);
+            trig[kTrigA + k] = ff_split(cv);
+            trig[kTrigA + kTrigB + k] = ff_split(sv);
+        }
     }
 }
+
+// Cosine by the split tables for k0 <= k < k0 + n (the tests compare it with
+// cos(2 pi k / 2^23) evaluated directly).
+__global__ void opinion_cos_check_kernel(const float2 *__restrict__ trig, int32_t k0, int32_t n, double *out)
+{
+    for (int32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const uint32_t k = (uint32_t)(k0 + q);
+        const float2 c = bm_cos_split(trig, k);
+        out[2 * q] = (double)c.x + (double)c.y;
+        out[2 * q + 1] = bm_cos(k);
+    }
+}
+
 // All of a row's loads are issued before the sums: for width 8 the weight row
 // is two 16-byte loads, then the (up to 8) neighbour indices, then their opinions.
 template <int W> // 8, or 0 for any width
@@ -415,9 +511,21 @@ __device__ __forceinline__ float opinion_mean(const SgTickArgs &a, const SgSeg &
         const float4 *w4 = reinterpret_cast<const float4 *>(sg.weights + (int64_t)i * 8);
         const float4 w0 = __ldcs(w4), w1 = __ldcs(w4 + 1);
         const float wv[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+        // the row's first 8 indices: vector loads when the row start allows
+        // (a warp's rows are contiguous, so each load instruction is dense)
         int32_t nb[8];
+        if (m == 8 && (b & 3) == 0) {
+            const int4 *p4 = reinterpret_cast<const int4 *>(a.idx + b);
+            const int4 v0 = __ldcs(p4), v1 = __ldcs(p4 + 1);
+            nb[0] = v0.x, nb[1] = v0.y, nb[2] = v0.z, nb[3] = v0.w, nb[4] = v1.x, nb[5] = v1.y, nb[6] = v1.z, nb[7] = v1.w;
+        } else if (m == 8 && (b & 1) == 0) {
+            const int2 *p2 = reinterpret_cast<const int2 *>(a.idx + b);
+            const int2 v0 = __ldcs(p2), v1 = __ldcs(p2 + 1), v2 = __ldcs(p2 + 2), v3 = __ldcs(p2 + 3);
+            nb[0] = v0.x, nb[1] = v0.y, nb[2] = v1.x, nb[3] = v1.y, nb[4] = v2.x, nb[5] = v2.y, nb[6] = v3.x, nb[7] = v3.y;
+        } else {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) nb[j] = j < m ? __ldcs(a.idx + b + j) : i;
+            for (int j = 0; j < 8; ++j) nb[j] = j < m ? __ldcs(a.idx + b + j) : i;
+        }
         float xv[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) xv[j] = __ldg(xin + nb[j]);
@@ -439,31 +547,133 @@ __device__ __forceinline__ float opinion_mean(const SgTickArgs &a, const SgSeg &
     return norm > 0.0f ? __fdiv_rn(acc, norm) : xin[i];
 }
 
-template <int W>
-__global__ void __launch_bounds__(SG_SIR_THREADS) opinion_kernel(SgTickArgs a)
+// Persistent blocks of kOpinionThreads threads (64 KiB of cosine tables in
+// shared memory each), work handed out round robin in chunks of one agent per
+// thread (any width) or, for width 8, two agents per thread: the opinion tick
+// is bound by the latency of its dependent loads (row bounds, then row
+// indices, then neighbour opinions), so a thread issues every load of a phase
+// for both of its agents before it waits on any, and the noise draw and its
+// radius load, which need no graph data, go first.
+constexpr int kOpinionThreads = 512;
+
+// Noise and clamp for one agent: y = x + sigma * radius * cos, rounded to
+// float32 and clamped to [0, 1]. Rounding is monotone and keeps 0 and 1, so
+// clamping after rounding gives the same value as clamping first; a negative
+// value rounds to a non-positive float, stored as +0.
+__device__ __forceinline__ float opinion_noise(const SgTickArgs &a, const SgSeg &sg, const float2 *trig, float x,
+                                               float2 r, uint32_t k1, uint32_t k2)
 {
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-        const SgTile tile = a.tiles[t];
+    float yf;
+    if (a.bm_radius && trig) {
+        const float2 c = bm_cos_split(trig, k2);
+        const float2 t = ff_mul(make_float2(a.sigma_hi, a.sigma_lo), ff_mul(r, c));
+        const float2 s2 = ff_two_sum(x, t.x); // x + t, rounded once
+        yf = ff_norm(s2.x, __fadd_rn(s2.y, t.y)).x;
+    } else {
+        const double z = __dmul_rn(bm_radius(k1), bm_cos(k2));
+        yf = __double2float_rn(__dadd_rn((double)x, __dmul_rn(sg.sigma, z)));
+    }
+    return yf <= 0.0f ? 0.0f : (yf > 1.0f ? 1.0f : yf);
+}
+
+template <int W>
+__global__ void __launch_bounds__(kOpinionThreads, W == 8 ? 2 : 3) opinion_kernel(SgTickArgs a)
+{
+    extern __shared__ float2 sh_trig[]; // SG_BM_TRIG_ENTRIES pairs when a.bm_trig is set
+    if (a.bm_trig) {
+        const float4 *src = reinterpret_cast<const float4 *>(a.bm_trig);
+        for (int j = threadIdx.x; j < SG_BM_TRIG_ENTRIES / 2; j += kOpinionThreads)
+            reinterpret_cast<float4 *>(sh_trig)[j] = __ldg(src + j);
+        __syncthreads();
+    }
+    const float2 *trig = a.bm_trig ? sh_trig : nullptr;
+    constexpr int32_t U = W == 8 ? 2 : 1;                      // agents per thread and chunk
+    constexpr int32_t parts = SG_TILE / (kOpinionThreads * U); // chunks per tile
+    const int32_t nchunks = a.ntiles * parts;
+    for (int32_t q = blockIdx.x; q < nchunks; q += gridDim.x) {
+        const SgTile tile = a.tiles[q / parts];
         const SgSeg &sg = a.segs[tile.seg];
         const int64_t tick = sg.tick0 + a.r;
-        if (tick >= sg.end_tick) continue;
+        if (tick >= sg.end_tick) continue; // the same for the whole block
         const int par = (sg.par0 + a.r) & 1;
         const float *__restrict__ xin = (const float *)(par ? a.buf1 : a.buf0);
         float *__restrict__ xout = (float *)(par ? a.buf0 : a.buf1);
         const uint32_t c0b = sg_c0base(tick);
-        const int32_t width = sg.width;
-        for (int32_t i = tile.begin + threadIdx.x; i < tile.end; i += SG_SIR_THREADS) {
-            const float x = opinion_mean<W>(a, sg, xin, i, width);
-            const uint32_t lid = seg_lid(sg, i);
-            const uint32_t k1 = sg_philox_k23(c0b + 1u, lid, sg.key);
-            const uint32_t k2 = sg_philox_k23(c0b + 1u + kNormalSalt2, lid, sg.key);
-            const double r = a.bm_radius ? __ldcs(a.bm_radius + k1) : bm_radius(k1);
-            const double c = a.bm_cos ? (a.l2_win ? __ldg(a.bm_cos + k2) : __ldcs(a.bm_cos + k2)) : bm_cos(k2);
-            const double z = __dmul_rn(r, c);
-            double y = __dadd_rn((double)x, __dmul_rn(sg.sigma, z));
-            if (y < 0.0) y = 0.0;
-            if (y > 1.0) y = 1.0;
-            xout[i] = (float)y;
+        int32_t iu[U];
+        bool vu[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int32_t i = tile.begin + (q % parts) * (kOpinionThreads * U) + u * kOpinionThreads +
+                              (int32_t)threadIdx.x;
+            vu[u] = i < tile.end;
+            iu[u] = vu[u] ? i : tile.begin; // a valid agent keeps every load in bounds
+        }
+        // 1. the normal draw's two Philox integers and the radius
+        uint32_t k1[U], k2[U];
+        float2 r[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t lid = seg_lid(sg, iu[u]);
+            k1[u] = sg_philox_k23(c0b + 1u, lid, sg.key);
+            k2[u] = sg_philox_k23(c0b + 1u + kNormalSalt2, lid, sg.key);
+            r[u] = make_float2(0.0f, 0.0f);
+            if (a.bm_radius) r[u] = a.l2_win ? __ldg(a.bm_radius + k1[u]) : __ldcs(a.bm_radius + k1[u]);
+        }
+        if (W != 8) {
+            const float x = opinion_mean<W>(a, sg, xin, iu[0], sg.width);
+            if (vu[0]) xout[iu[0]] = opinion_noise(a, sg, trig, x, r[0], k1[0], k2[0]);
+            continue;
+        }
+        // 2. row bounds, weights (read once per tick: evict-first loads keep L2
+        //    for the opinions, which neighbours re-read) and own opinions
+        int32_t b[U], m[U];
+        float wv[U][8], xo[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            b[u] = __ldg(a.off + iu[u]);
+            m[u] = min(__ldg(a.off + iu[u] + 1) - b[u], 8);
+            const float4 *w4 = reinterpret_cast<const float4 *>(sg.weights + (int64_t)iu[u] * 8);
+            const float4 w0 = __ldcs(w4), w1 = __ldcs(w4 + 1);
+            wv[u][0] = w0.x, wv[u][1] = w0.y, wv[u][2] = w0.z, wv[u][3] = w0.w;
+            wv[u][4] = w1.x, wv[u][5] = w1.y, wv[u][6] = w1.z, wv[u][7] = w1.w;
+            xo[u] = xin[iu[u]];
+        }
+        // 3. the rows' first 8 indices (8-byte loads when the row start allows;
+        //    a warp's rows are contiguous, so each load instruction is dense)
+        int32_t nb[U][8];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (m[u] == 8 && (b[u] & 1) == 0) {
+                const int2 *p2 = reinterpret_cast<const int2 *>(a.idx + b[u]);
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    const int2 v = __ldcs(p2 + h);
+                    nb[u][2 * h] = v.x;
+                    nb[u][2 * h + 1] = v.y;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 8; ++j) nb[u][j] = j < m[u] ? __ldcs(a.idx + b[u] + j) : iu[u];
+            }
+        }
+        // 4. neighbour opinions
+        float xv[U][8];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) xv[u][j] = __ldg(xin + nb[u][j]);
+        // 5. weighted mean in row order (every multiply and add rounded), noise, store
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            float acc = 0.0f, norm = 0.0f;
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                if (j < m[u]) {
+                    acc = __fadd_rn(acc, __fmul_rn(wv[u][j], xv[u][j]));
+                    norm = __fadd_rn(norm, fabsf(wv[u][j]));
+                }
+            const float x = norm > 0.0f ? __fdiv_rn(acc, norm) : xo[u];
+            if (vu[u]) xout[iu[u]] = opinion_noise(a, sg, trig, x, r[u], k1[u], k2[u]);
         }
     }
 }
@@ -557,34 +767,54 @@ static int stride_grid(int64_t work)
     return (int)(b < 1 ? 1 : b > cap ? cap : b);
 }
 
-cudaError_t sg_launch_opinion_tables(double *radius, double *cosine, cudaStream_t st)
+cudaError_t sg_launch_opinion_tables(float2 *radius, float2 *trig, cudaStream_t st)
 {
-    opinion_tables_kernel<<<current_sm_count() * 8, 256, 0, st>>>(radius, cosine);
+    opinion_tables_kernel<<<current_sm_count() * 8, 256, 0, st>>>(radius, trig);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_launch_opinion_cos_check(const float2 *trig, int32_t k0, int32_t n, double *out, cudaStream_t st)
+{
+    opinion_cos_check_kernel<<<current_sm_count() * 8, 256, 0, st>>>(trig, k0, n, out);
     return cudaGetLastError();
 }
 
 // width: the weights per agent of every segment of the launch (8 takes the
-// vector-load path).
+// vector-load path). The grid is three persistent blocks per SM (the `grid`
+// argument caps it).
 cudaError_t sg_launch_opinion(const SgTickArgs &a, int grid, cudaStream_t st, int width)
 {
     void (*k)(SgTickArgs) = width == 8 ? opinion_kernel<8> : opinion_kernel<0>;
-    if (!a.l2_win) {
-        k<<<grid, SG_SIR_THREADS, 0, st>>>(a);
-        return cudaGetLastError();
-    }
+    const size_t smem = a.bm_trig ? (size_t)SG_BM_TRIG_ENTRIES * sizeof(float2) : 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute(opinion_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(SG_BM_TRIG_ENTRIES * sizeof(float2)));
+        cudaFuncSetAttribute(opinion_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(SG_BM_TRIG_ENTRIES * sizeof(float2)));
+    });
+    const int per_thread = width == 8 ? 2 : 1;
+    const int64_t nchunks = (int64_t)a.ntiles * (SG_TILE / (kOpinionThreads * per_thread));
+    int64_t g = (int64_t)current_sm_count() * (width == 8 ? 2 : 3); // resident blocks per SM
+    if (g > nchunks) g = nchunks;
+    if (grid > 0 && g > (int64_t)grid * 4) g = (int64_t)grid * 4;
+    if (g < 1) g = 1;
     cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3(SG_SIR_THREADS);
+    cfg.gridDim = dim3((unsigned)g);
+    cfg.blockDim = dim3(kOpinionThreads);
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute at{};
-    at.id = cudaLaunchAttributeAccessPolicyWindow;
-    at.val.accessPolicyWindow.base_ptr = const_cast<void *>(a.l2_win);
-    at.val.accessPolicyWindow.num_bytes = a.l2_win_bytes;
-    at.val.accessPolicyWindow.hitRatio = a.l2_win_hit;
-    at.val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
-    at.val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
-    cfg.attrs = &at;
-    cfg.numAttrs = 1;
+    if (a.l2_win) {
+        at.id = cudaLaunchAttributeAccessPolicyWindow;
+        at.val.accessPolicyWindow.base_ptr = const_cast<void *>(a.l2_win);
+        at.val.accessPolicyWindow.num_bytes = a.l2_win_bytes;
+        at.val.accessPolicyWindow.hitRatio = a.l2_win_hit;
+        at.val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+        at.val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+        cfg.attrs = &at;
+        cfg.numAttrs = 1;
+    }
     return cudaLaunchKernelEx(&cfg, k, a);
 }
 

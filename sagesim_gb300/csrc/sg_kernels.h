@@ -52,7 +52,10 @@ struct SgMega {
 #define SG_FLAVOUR_HYBRID 256 // class sweep in quiet ticks, the loop form (bits 0-2) in
                               // busy ticks (see SgTickArgs::hybrid_rise/fall and
                               // sg_hybrid_thresholds)
-#define SG_FLAVOUR_MAX 511
+#define SG_FLAVOUR_FLAT 512   // flat draws in place of the loop form (in-place runs): a
+                              // block lays its tile's draws end to end and each thread
+                              // takes an equal share
+#define SG_FLAVOUR_MAX 1023
 // The class sweep runs one warp per tile; below this many tiles per SM it
 // leaves SMs idle and the loop form (lazy loads) is used instead, unless
 // SG_FLAVOUR_FORCE is set.
@@ -140,11 +143,12 @@ struct SgTickArgs {
     int32_t sweep_wpt;      // class sweep: warps per tile (1, 2 or 4; see sg_sweep_wpt)
     size_t cnt_window;      // count strategy: bytes of cnt to keep in L2 as persisting lines
                             // (an access-policy window on the count kernels); 0 = none
-    const double *bm_radius; // opinion: NULL, or the 2^23-entry Box-Muller tables of
-    const double *bm_cos;    // sg_launch_opinion_tables
+    const float2 *bm_radius; // opinion: NULL, or the 2^23-entry Box-Muller radius table and
+    const float2 *bm_trig;   // the split cosine tables of sg_launch_opinion_tables
+    float sigma_hi, sigma_lo; // opinion: the noise sigma as a double-float pair (with the tables)
     const void *l2_win;     // opinion: NULL, or an access-policy window (persisting lines)
     size_t l2_win_bytes;    // over l2_win_bytes from l2_win, a fraction l2_win_hit of its
-    float l2_win_hit;       // lines kept (the cosine table, read at random)
+    float l2_win_hit;       // lines kept (the radius table, read at random)
     int32_t hybrid_rise;    // hybrid count step (0 = off): tick r > 1 runs the loop form
     int32_t hybrid_fall;    // when tick r - 1 recorded more than hybrid_rise changes and
                             // no fewer than tick r - 2 (epidemic growing), or more than
@@ -184,10 +188,18 @@ cudaError_t sg_launch_frontier_build(const SgTickArgs &a, bool stats, int grid, 
 cudaError_t sg_launch_frontier_step(const SgTickArgs &a, int variant, bool stats, int grid, cudaStream_t st);
 cudaError_t sg_launch_frontier_scatter(const SgTickArgs &a, int grid, cudaStream_t st);
 cudaError_t sg_launch_opinion(const SgTickArgs &a, int grid, cudaStream_t st, int width);
-// Fills the opinion step's Box-Muller tables, 2^23 doubles each (64 MiB each):
-// radius[k] = sqrt(-2 log(k / 2^23 + 1e-10)), cosine[k] = cos(2 pi k / 2^23).
+// Fills the opinion step's Box-Muller tables, each entry a double-float pair
+// (hi, lo) of float32: radius[k] = sqrt(-2 log(k / 2^23 + 1e-10)) for k < 2^23
+// (64 MiB), and trig = SG_BM_TRIG_ENTRIES pairs: cos of 2 pi j / 2^12 (j < 4096),
+// then cos and sin of 2 pi l / 2^23 (l < 2048), from which the step forms
+// cos(2 pi k / 2^23) by angle addition. radius may be NULL: only the cosine
+// tables are filled.
 #define SG_BOX_MULLER_SIZE (1 << 23)
-cudaError_t sg_launch_opinion_tables(double *radius, double *cosine, cudaStream_t st);
+#define SG_BM_TRIG_ENTRIES (4096 + 2 * 2048)
+cudaError_t sg_launch_opinion_tables(float2 *radius, float2 *trig, cudaStream_t st);
+// out[2 q] = the split-table cosine of k = k0 + q (hi + lo), out[2 q + 1] =
+// cos(2 pi k / 2^23) evaluated directly (q < n).
+cudaError_t sg_launch_opinion_cos_check(const float2 *trig, int32_t k0, int32_t n, double *out, cudaStream_t st);
 // Adds edge_base to off[0..n1) and agent_base to idx[0..nnz) in place (placing a
 // scenario's local CSR into a pool).
 cudaError_t sg_launch_offset_csr(int32_t *off, int64_t n1, int32_t edge_base, int32_t *idx, int64_t nnz,

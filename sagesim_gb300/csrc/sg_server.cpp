@@ -25,6 +25,8 @@ struct Request {
     std::vector<int64_t> lids;
     int64_t bytes = 0;
     int32_t status = SG_REQ_QUEUED;
+    bool borrowed = false; // d's host pointers are the caller's (SG_REQ_BORROW), no copies
+    std::string failure;   // SG_REQ_FAILED: why placement refused it
     int32_t bypassed = 0;
     int64_t tick = 0;
     std::vector<int32_t> result;
@@ -55,13 +57,24 @@ static int admit(sg_server *s)
         const bool budget_ok = s->resident_bytes + r.bytes <= s->cfg.budget_bytes;
         if (!blocked && budget_ok && p.fits(r.d.n_agents, r.d.nnz)) {
             const int32_t sid = s->next_sid++;
-            int rc = p.place(r.d, r.off.data(), r.idx.data(), r.state.data(),
-                             r.lids.empty() ? nullptr : r.lids.data(), sid);
+            int rc = r.borrowed ? p.place(r.d, r.d.offsets, r.d.indices, r.d.state, r.d.lids, sid, true)
+                                : p.place(r.d, r.off.data(), r.idx.data(), r.state.data(),
+                                          r.lids.empty() ? nullptr : r.lids.data(), sid);
             if (rc == SG_ERR_BUDGET) { // fragmentation: try later
                 ++it;
                 continue;
             }
+            if (rc == SG_ERR_BAD_CSR && r.borrowed) { // checked on the device only now
+                r.status = SG_REQ_FAILED;
+                r.failure = p.err;
+                r.d.offsets = r.d.indices = r.d.state = nullptr;
+                r.d.lids = nullptr;
+                it = s->queue.erase(it);
+                continue;
+            }
             if (rc) return rc;
+            r.d.offsets = r.d.indices = r.d.state = nullptr; // the caller's arrays are free again
+            r.d.lids = nullptr;
             s->rid_sid[r.rid] = sid;
             s->resident_bytes += r.bytes;
             r.status = SG_REQ_RUNNING;
@@ -194,6 +207,17 @@ int sg_server_submit(sg_server *s, const sg_scenario_desc *d, int64_t *rid)
         if (rc != SG_ERR_BUDGET) return rc; // SG_ERR_BAD_CSR from the device check, or a CUDA error
         // fragmented pool: queue it
     }
+    if (d->flags & SG_REQ_BORROW) { // the caller keeps the arrays: no check or copy on the host
+        auto r = std::make_unique<Request>();
+        r->rid = s->next_rid++;
+        r->d = *d;
+        r->borrowed = true;
+        r->bytes = bytes;
+        *rid = r->rid;
+        s->queue.push_back(r->rid);
+        s->reqs[r->rid] = std::move(r);
+        return SG_OK;
+    }
     std::string why = sg_check_csr(d->offsets, d->n_agents, d->indices, d->nnz);
     if (!why.empty()) return s->pool.fail(SG_ERR_BAD_CSR, why);
     auto r = std::make_unique<Request>();
@@ -246,6 +270,11 @@ int sg_server_take_result(sg_server *s, int64_t rid, int32_t *host, int64_t n)
     auto it = s->reqs.find(rid);
     if (it == s->reqs.end()) return s->pool.fail(SG_ERR_NOT_FOUND, "unknown request id");
     Request &r = *it->second;
+    if (r.status == SG_REQ_FAILED) {
+        const std::string why = r.failure;
+        s->reqs.erase(it);
+        return s->pool.fail(SG_ERR_BAD_CSR, "request refused when placed: " + why);
+    }
     if (r.status != SG_REQ_DONE) return s->pool.fail(SG_ERR_INVALID, "request not finished");
     if (n != r.d.n_agents) return s->pool.fail(SG_ERR_INVALID, "n differs from the request's agent count");
     memcpy(host, r.result.data(), (size_t)n * 4);

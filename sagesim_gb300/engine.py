@@ -232,10 +232,17 @@ class Engine:
     def restore(self):
         self._ck(self._lib.sg_restore(self._h))
 
-    def set_tune(self, blocks_per_sm=16, thread_row=32, mega_row=2048, count_flavour=278):
+    def set_tune(self, blocks_per_sm=16, thread_row=32, mega_row=2048, count_flavour=790):
         """Launch configuration of the SIR kernels (results are identical for all)."""
         t = N.Tune(N.SG_SIR_COUNT, blocks_per_sm, thread_row, mega_row, count_flavour, 0.0)
         self._ck(self._lib.sg_engine_set_tune(self._h, ctypes.byref(t)))
+
+    def opinion_cosine_check(self, k0, n):
+        """(split-table cosine, direct cos) of 2 pi k / 2^23 for k0 <= k < k0 + n."""
+        split = np.empty(n, dtype=np.float64)
+        direct = np.empty(n, dtype=np.float64)
+        self._ck(self._lib.sg_opinion_cosine_check(self._h, int(k0), int(n), _ptr(split), _ptr(direct)))
+        return split, direct
 
     def profile(self, on=True):
         self._ck(self._lib.sg_profile_enable(self._h, 1 if on else 0))

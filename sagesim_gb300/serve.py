@@ -29,6 +29,7 @@ class Server:
         self._h = h
         self.variant = variant
         self._n = {}
+        self._borrowed = {}  # rid -> arrays a borrowed request points into
 
     def _ck(self, rc):
         return N.check(rc, self._h, "sg_server_last_error")
@@ -37,6 +38,7 @@ class Server:
         if getattr(self, "_h", None):
             self._lib.sg_server_destroy(self._h)
             self._h = None
+        self._borrowed = {}
 
     def __del__(self):
         try:
@@ -50,16 +52,25 @@ class Server:
     def __exit__(self, *exc):
         self.close()
 
-    def submit(self, offsets, indices, state, seed, beta, gamma, horizon, codes=(1, 2, 3), lids=None):
+    def submit(self, offsets, indices, state, seed, beta, gamma, horizon, codes=(1, 2, 3), lids=None,
+               borrow=False):
         """Queues (or places at once) one scenario. lids: the logical id of every
         agent, the key of its random draws (sagesim/model.py:656-667); None keys
-        the draws on the agent index, as the reference does by default."""
+        the draws on the agent index, as the reference does by default.
+        borrow: the arrays stay valid and unchanged until the request is placed
+        (the server keeps references to them until its result is taken), so a
+        queued request is neither copied nor checked on the host; its CSR is
+        checked on the device when it is placed."""
         keep = []
         d = scenario_desc(offsets, indices, state, seed, beta, gamma, self.variant, horizon, lids, codes,
                           True, keep)
+        if borrow:
+            d.flags |= N.SG_REQ_BORROW
         rid = ctypes.c_int64()
         self._ck(self._lib.sg_server_submit(self._h, ctypes.byref(d), ctypes.byref(rid)))
         self._n[rid.value] = d.n_agents
+        if borrow:
+            self._borrowed[rid.value] = keep
         return rid.value
 
     def step(self, nticks):
@@ -74,6 +85,7 @@ class Server:
 
     def take_result(self, rid):
         out = np.empty(self._n.pop(rid), dtype=np.int32)
+        self._borrowed.pop(rid, None)
         self._ck(self._lib.sg_server_take_result(self._h, rid, ctypes.c_void_p(out.ctypes.data), out.size))
         return out
 
@@ -88,11 +100,13 @@ class Server:
         self._ck(self._lib.sg_server_set_tune(self._h, ctypes.byref(t)))
 
 
-def serve_stream(server, requests, arrivals, chunk=8, keep_results=True, clock=time.perf_counter):
+def serve_stream(server, requests, arrivals, chunk=8, keep_results=True, clock=time.perf_counter, borrow=False):
     """Submits requests[i] (dict of Server.submit kwargs) at arrivals[i] seconds
     after the start, steps the server by `chunk` ticks while work remains, and
     returns per-request latency (completion - arrival, seconds), results and totals
-    (with the host time spent in submit and in step)."""
+    (with the host time spent in submit and in step). keep_results: keep every
+    result (True), none (False) or those whose index is in the given set.
+    borrow: submit with borrow=True (the requests' arrays outlive the stream)."""
     order = np.argsort(arrivals, kind="stable")
     t0 = clock()
     rid_of, req_of = {}, {}
@@ -107,7 +121,7 @@ def serve_stream(server, requests, arrivals, chunk=8, keep_results=True, clock=t
         while nxt < len(order) and arrivals[order[nxt]] <= now:
             i = int(order[nxt])
             ts = clock()
-            rid = server.submit(**requests[i])
+            rid = server.submit(**requests[i], borrow=True) if borrow else server.submit(**requests[i])
             t_submit += clock() - ts
             rid_of[i] = rid
             req_of[rid] = i
@@ -126,11 +140,11 @@ def serve_stream(server, requests, arrivals, chunk=8, keep_results=True, clock=t
             tnow = clock() - t0
             for rid in list(req_of):
                 st, _ = server.poll(rid)
-                if st == N.SG_REQ_DONE:
+                if st in (N.SG_REQ_DONE, N.SG_REQ_FAILED):
                     i = req_of.pop(rid)
                     done_at[i] = tnow
-                    res = server.take_result(rid)
-                    if keep_results:
+                    res = server.take_result(rid)  # raises for a request refused at placement
+                    if keep_results is True or (keep_results and i in keep_results):
                         results[i] = res
                     agent_ticks += res.size * int(requests[i]["horizon"])
                     pending -= 1

@@ -62,7 +62,7 @@ def test_batch_scenarios_match_standalone(strategy, variant):
 
 
 @pytest.mark.parametrize("flavours", [(48, 0, 48 | 64), (0, 48 | 128, 4), (56, 5, 49), (16, 0, 16), (48 | 256 | 4, 0, 48 | 256),
-                                      (6, 48 | 256 | 6, 2)])
+                                      (6, 48 | 256 | 6, 2), (48 | 256 | 512, 512, 4), (512, 48, 48 | 256 | 512 | 6)])
 def test_batch_count_flavours_switch_between_runs(flavours):
     """Class bytes are kept by every count-strategy kernel and the activity bits
     are rebuilt at the start of every run, so the class sweep can take over from

@@ -83,7 +83,10 @@ def test_sir_matches_oracle_every_tick(variant, strategy, kind):
 
 
 COUNT_FLAVOURS = list(range(8)) + [8, 12, 16, 24, 48, 56, 63, 48 | 64, 48 | 128, 56 | 192, 48 | 256 | 4, 48 | 256 | 1,
-                                   16 | 256, 48 | 256 | 6, 16 | 256 | 6]
+                                   16 | 256, 48 | 256 | 6, 16 | 256 | 6,
+                                   # flat draws: every tick, every tick with a row-per-lane scatter, and in
+                                   # the hybrid's busy ticks (forced on this small graph)
+                                   512, 512 | 8, 512 | 48 | 256, 512 | 48 | 256 | 6]
 
 
 @pytest.mark.parametrize("flavour", COUNT_FLAVOURS)
@@ -109,7 +112,8 @@ def test_count_step_flavours_identical(flavour, variant):
     assert np.array_equal(got, ref)
 
 
-@pytest.mark.parametrize("flavour", [0, 16, 48, 48 | 64, 48 | 128, 48 | 256 | 4, 48 | 256 | 3, 48 | 256 | 6])
+@pytest.mark.parametrize("flavour", [0, 16, 48, 48 | 64, 48 | 128, 48 | 256 | 4, 48 | 256 | 3, 48 | 256 | 6,
+                                     512, 512 | 48 | 256])
 @pytest.mark.parametrize("variant", ["A", "B"])
 def test_count_dense_graph_with_statistics(flavour, variant):
     """A dense graph with many infected neighbours per agent and a small beta
@@ -130,6 +134,30 @@ def test_count_dense_graph_with_statistics(flavour, variant):
     ref, rstats, _ = oracle.sir_run(1 if variant == "A" else 2, off, idx, st0, 11, 0, 12, beta, gamma)
     assert np.array_equal(got, ref)
     assert np.array_equal(stats, rstats)
+
+
+@pytest.mark.parametrize("variant", ["A", "B"])
+def test_flat_step_on_a_range_without_class_bytes(variant):
+    """A count step over agents [37, n - 100): its tiles do not start at
+    multiples of 32, so no class bytes are kept and the flat-draw step reads the
+    states (scalar loads at unaligned tile edges); agents outside the range keep
+    their state. Equal to the loop form, every tick's statistics included."""
+    off, idx = hub_graph(9)
+    n = off.size - 1
+    st0 = _init_state(n, 0.02, 9)
+    out = {}
+    for fl in (4, 512):
+        with Engine() as e:
+            e.set_graph(off, idx, symmetric=True)
+            e.set_seed(3)
+            p = e.add_property("state", np.int32, init=st0)
+            e.add_sir(p, 0.05, 0.08, variant=variant, strategy="count", begin=37, end=n - 100)
+            e.set_tune(count_flavour=fl)
+            stats, _ = e.run(0, 40, stats=True)
+            out[fl] = (e.get_property(p), stats)
+    assert np.array_equal(out[4][0], out[512][0]) and np.array_equal(out[4][1], out[512][1])
+    assert np.array_equal(out[512][0][:37], st0[:37]) and np.array_equal(out[512][0][n - 100:], st0[n - 100:])
+    assert not np.array_equal(out[512][0], st0)
 
 
 @pytest.mark.parametrize("wpt_bits", [64, 128, 192, 256 | 4, 256 | 64 | 2])

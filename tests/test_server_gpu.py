@@ -50,7 +50,7 @@ def test_poll_and_take_result():
     with Server(budget_bytes=1 << 30, agent_slots=1_000_000, edge_slots=10_000_000) as srv:
         srv.set_tune()  # the defaults (class sweep + hybrid step) are accepted
         with pytest.raises(SageSimError):
-            srv.set_tune(count_flavour=512)
+            srv.set_tune(count_flavour=1024)
         rid = srv.submit(**r)
         assert srv.poll(rid) == (1, 0)  # room at once: placed on the device, running
         srv.step(5)
@@ -137,3 +137,35 @@ def test_requests_with_logical_ids_alone_and_in_the_mix():
                                     o["beta"], o["gamma"])
         got = out["results"][i] if perms[i] is None else out["results"][i][perms[i]]
         assert np.array_equal(got, want), "request %d against the oracle" % i
+
+
+def test_borrowed_requests_queue_without_host_copies():
+    """Requests submitted with borrow=True: those that queue keep the caller's
+    arrays (no host copy or host CSR pass) and are checked on the device when
+    placed. Results equal the standalone runs; a borrowed request with a bad CSR
+    that queued is refused at placement (status SG_REQ_FAILED, take_result
+    raises SG_ERR_BAD_CSR) without disturbing the others."""
+    from sagesim_gb300 import _native as N
+
+    reqs = requests(10, 16)
+    bad = dict(reqs[3], indices=reqs[3]["indices"].copy())
+    bad["indices"][5] = bad["offsets"].size + 7  # outside [0, n)
+    budget = est_bytes(reqs[0]) + 1  # one resident at a time: the rest queue
+    with Server(budget_bytes=max(budget, max(est_bytes(r) for r in reqs) + 1), agent_slots=2_000_000,
+                edge_slots=40_000_000) as srv:
+        rids = [srv.submit(**r, borrow=True) for r in reqs]
+        bad_rid = srv.submit(**bad, borrow=True)
+        assert srv.poll(bad_rid)[0] == N.SG_REQ_QUEUED
+        pending = set(rids)
+        results = {}
+        while pending or srv.poll(bad_rid)[0] == N.SG_REQ_QUEUED:
+            srv.step(32)
+            for rid in list(pending):
+                if srv.poll(rid)[0] == N.SG_REQ_DONE:
+                    results[rid] = srv.take_result(rid)
+                    pending.discard(rid)
+        assert srv.poll(bad_rid)[0] == N.SG_REQ_FAILED
+        with pytest.raises(SageSimError, match="BAD_CSR"):
+            srv.take_result(bad_rid)
+    for rid, r in zip(rids, reqs):
+        assert np.array_equal(results[rid], standalone(r, "B", r["horizon"])), rid
