@@ -485,7 +485,7 @@ def serving_section(stream, device=0, n_requests=1000, n_graphs=64):
             "oracle_checked": {"requests": len(sample), "bit_exact": oracle_ok}}
 
 
-def algorithmic_bytes(kernel, n, st0, tick_stats, active):
+def algorithmic_bytes(kernel, n, st0, tick_stats, active, flat=True):
     """Compulsory DRAM bytes per launch of `kernel`, per tick of the run (int32 state).
 
     sir_pull          12 B per agent (state read/write, row offset) + 4 B per CSR
@@ -495,9 +495,12 @@ def algorithmic_bytes(kernel, n, st0, tick_stats, active):
                       (active[] = infected agents + susceptible agents with the
                       bit set), 4 B count per susceptible candidate, 9 B per
                       transition (state write, class write, change entry);
-                      loop-form ticks (hybrid step in busy ticks): 4 B state read
-                      per agent, 4 B count read per tick-start S agent, 8 B per
-                      transition
+                      busy ticks (hybrid step): with flat draws (the default), 1 B
+                      class read per agent, 4 B count per tick-start S agent, 4 B
+                      RNG key per candidate (at most the tick-start I and S
+                      agents: counted as all of them), 9 B per transition; with
+                      the loop form, 4 B state read per agent, 4 B count read per
+                      tick-start S agent, 8 B per transition
     frontier_step     20 B per active agent (list, state, count, mark, next list)
                       + 8 B per transition
     *_scatter         8 B per transition (change entry, transpose offsets) + 12 B
@@ -523,8 +526,11 @@ def algorithmic_bytes(kernel, n, st0, tick_stats, active):
         I = tick_stats[:, 1].astype(np.float64)
         I_start = np.concatenate([[float((st0 == CODES[1]).sum())], I[:-1]])
         sweep = 1.125 * n + 4.0 * active + 4.0 * np.maximum(active - I_start, 0.0) + 9.0 * changes
-        loop = 4.0 * n + 4.0 * S_start + 8.0 * changes
-        return np.where(active >= n, loop, sweep)
+        if flat:
+            busy = 1.0 * n + 4.0 * S_start + 4.0 * (I_start + S_start) + 9.0 * changes
+        else:
+            busy = 4.0 * n + 4.0 * S_start + 8.0 * changes
+        return np.where(active >= n, busy, sweep)
     if kernel == "frontier_step":
         return 20.0 * active + 8.0 * changes
     if kernel in ("sir_count_scatter", "frontier_scatter"):

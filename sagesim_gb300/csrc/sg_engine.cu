@@ -86,6 +86,8 @@ struct sg_engine {
     SgDev transpose_tmp, scan_tmp;
     SgDev bm_radius, bm_trig; // opinion: Box-Muller tables, built once per engine
     bool bm_ready = false;
+    SgDev nb8;               // opinion (width 8): first 8 neighbours per agent, column-major, -1 padded
+    bool nb8_valid = false;  // nb8 matches the current graph
     bool l2_limit_set = false;
     SgDev prop_table; // sg_prop_dev per property, for compiled steps
 
@@ -255,6 +257,7 @@ int sg_set_graph_csr(sg_engine *e, const int32_t *offsets, int64_t n, const int3
     e->nnz = nnz;
     e->graph_flags = flags;
     e->have_transpose = false;
+    e->nb8_valid = false;
     e->version++;
     return SG_OK;
 }
@@ -298,6 +301,7 @@ int sg_set_graph_id_edges(sg_engine *e, const int64_t *ids, int64_t n, const int
     e->nnz = nnz;
     e->graph_flags = flags & (SG_GRAPH_SYMMETRIC | SG_GRAPH_ORDERED);
     e->have_transpose = false;
+    e->nb8_valid = false;
     e->version++;
     return SG_OK;
 }
@@ -791,6 +795,8 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
             } else if (s->kind == SG_BUILTIN_OPINION) {
                 a.bm_radius = e->bm_ready ? e->bm_radius.as<float2>() : nullptr;
                 a.bm_trig = e->bm_ready ? e->bm_trig.as<float2>() : nullptr;
+                a.nb8 = e->nb8_valid && s->host_seg.width == 8 ? e->nb8.as<int32_t>() : nullptr;
+                a.nb8_stride = e->n;
                 {
                     const double sg = s->bp.sigma;
                     a.sigma_hi = (float)sg;
@@ -890,6 +896,13 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
             SG_CK(e->bm_trig.reserve((size_t)SG_BM_TRIG_ENTRIES * sizeof(float2)));
             SG_CK(sg_launch_opinion_tables(e->bm_radius.as<float2>(), e->bm_trig.as<float2>(), e->stream));
             e->bm_ready = true;
+        }
+        if (s->kind == SG_BUILTIN_OPINION && s->host_seg.width == 8 && !e->nb8_valid && e->n > 0) {
+            // the neighbour table of the width-8 opinion step, rebuilt with the graph
+            SG_CK(e->nb8.reserve((size_t)e->n * 8 * sizeof(int32_t)));
+            SG_CK(sg_launch_opinion_neighbours8(e->off.as<int32_t>(), e->idx.as<int32_t>(), e->n,
+                                                e->nb8.as<int32_t>(), e->stream));
+            e->nb8_valid = true;
         }
     }
     if (pl.count_step) {

@@ -483,6 +483,18 @@ __global__ void opinion_tables_kernel(float2 *__restrict__ radius, float2 *__res
     }
 }
 
+// First 8 neighbours of every agent, column-major, -1 after the row ends.
+__global__ void opinion_neighbours8_kernel(const int32_t *__restrict__ off, const int32_t *__restrict__ idx,
+                                           int64_t n, int32_t *__restrict__ nb8)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t b = off[i];
+        const int32_t m = min(off[i + 1] - b, 8);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) nb8[j * n + i] = j < m ? idx[b + j] : -1;
+    }
+}
+
 // Cosine by the split tables for k0 <= k < k0 + n (the tests compare it with
 // cos(2 pi k / 2^23) evaluated directly).
 __global__ void opinion_cos_check_kernel(const float2 *__restrict__ trig, int32_t k0, int32_t n, double *out)
@@ -619,41 +631,38 @@ __global__ void __launch_bounds__(kOpinionThreads, W == 8 ? 2 : 3) opinion_kerne
             r[u] = make_float2(0.0f, 0.0f);
             if (a.bm_radius) r[u] = a.l2_win ? __ldg(a.bm_radius + k1[u]) : __ldcs(a.bm_radius + k1[u]);
         }
-        if (W != 8) {
-            const float x = opinion_mean<W>(a, sg, xin, iu[0], sg.width);
-            if (vu[0]) xout[iu[0]] = opinion_noise(a, sg, trig, x, r[0], k1[0], k2[0]);
+        if (W != 8 || !a.nb8) { // any width, or no neighbour table: one agent at a time
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const float x = opinion_mean<0>(a, sg, xin, iu[u], sg.width);
+                if (vu[u]) xout[iu[u]] = opinion_noise(a, sg, trig, x, r[u], k1[u], k2[u]);
+            }
             continue;
         }
-        // 2. row bounds, weights (read once per tick: evict-first loads keep L2
-        //    for the opinions, which neighbours re-read) and own opinions
-        int32_t b[U], m[U];
+        // 2. weights (read once per tick: evict-first loads keep L2 for the
+        //    opinions, which neighbours re-read), own opinions, and the first 8
+        //    neighbours from the column-major table (each load instruction of a
+        //    warp is one 128-byte line)
+        int32_t m[U], nb[U][8];
         float wv[U][8], xo[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            b[u] = __ldg(a.off + iu[u]);
-            m[u] = min(__ldg(a.off + iu[u] + 1) - b[u], 8);
             const float4 *w4 = reinterpret_cast<const float4 *>(sg.weights + (int64_t)iu[u] * 8);
             const float4 w0 = __ldcs(w4), w1 = __ldcs(w4 + 1);
             wv[u][0] = w0.x, wv[u][1] = w0.y, wv[u][2] = w0.z, wv[u][3] = w0.w;
             wv[u][4] = w1.x, wv[u][5] = w1.y, wv[u][6] = w1.z, wv[u][7] = w1.w;
             xo[u] = xin[iu[u]];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) nb[u][j] = __ldcs(a.nb8 + j * a.nb8_stride + iu[u]);
         }
-        // 3. the rows' first 8 indices (8-byte loads when the row start allows;
-        //    a warp's rows are contiguous, so each load instruction is dense)
-        int32_t nb[U][8];
+        // 3. the row length is the count of valid entries (they come first)
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            if (m[u] == 8 && (b[u] & 1) == 0) {
-                const int2 *p2 = reinterpret_cast<const int2 *>(a.idx + b[u]);
+            m[u] = 0;
 #pragma unroll
-                for (int h = 0; h < 4; ++h) {
-                    const int2 v = __ldcs(p2 + h);
-                    nb[u][2 * h] = v.x;
-                    nb[u][2 * h + 1] = v.y;
-                }
-            } else {
-#pragma unroll
-                for (int j = 0; j < 8; ++j) nb[u][j] = j < m[u] ? __ldcs(a.idx + b[u] + j) : iu[u];
+            for (int j = 0; j < 8; ++j) {
+                m[u] += nb[u][j] >= 0;
+                if (nb[u][j] < 0) nb[u][j] = iu[u];
             }
         }
         // 4. neighbour opinions
@@ -770,6 +779,14 @@ static int stride_grid(int64_t work)
 cudaError_t sg_launch_opinion_tables(float2 *radius, float2 *trig, cudaStream_t st)
 {
     opinion_tables_kernel<<<current_sm_count() * 8, 256, 0, st>>>(radius, trig);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_launch_opinion_neighbours8(const int32_t *offsets, const int32_t *indices, int64_t n, int32_t *nb8,
+                                          cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    opinion_neighbours8_kernel<<<stride_grid(n), 256, 0, st>>>(offsets, indices, n, nb8);
     return cudaGetLastError();
 }
 

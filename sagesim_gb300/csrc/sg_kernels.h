@@ -146,6 +146,8 @@ struct SgTickArgs {
     const float2 *bm_radius; // opinion: NULL, or the 2^23-entry Box-Muller radius table and
     const float2 *bm_trig;   // the split cosine tables of sg_launch_opinion_tables
     float sigma_hi, sigma_lo; // opinion: the noise sigma as a double-float pair (with the tables)
+    const int32_t *nb8;     // opinion, width 8: NULL, or nb8[j * nb8_stride + i] = the j-th
+    int64_t nb8_stride;     // neighbour of agent i for j < min(deg, 8), -1 after (column-major)
     const void *l2_win;     // opinion: NULL, or an access-policy window (persisting lines)
     size_t l2_win_bytes;    // over l2_win_bytes from l2_win, a fraction l2_win_hit of its
     float l2_win_hit;       // lines kept (the radius table, read at random)
@@ -197,6 +199,11 @@ cudaError_t sg_launch_opinion(const SgTickArgs &a, int grid, cudaStream_t st, in
 #define SG_BOX_MULLER_SIZE (1 << 23)
 #define SG_BM_TRIG_ENTRIES (4096 + 2 * 2048)
 cudaError_t sg_launch_opinion_tables(float2 *radius, float2 *trig, cudaStream_t st);
+// nb8[j * n + i] = indices[offsets[i] + j] for j < min(deg(i), 8), else -1: the
+// width-8 opinion step's neighbours in a column-major table, so that a warp's
+// loads of the j-th neighbours of 32 consecutive agents are one 128-byte line.
+cudaError_t sg_launch_opinion_neighbours8(const int32_t *offsets, const int32_t *indices, int64_t n, int32_t *nb8,
+                                          cudaStream_t st);
 // out[2 q] = the split-table cosine of k = k0 + q (hi + lo), out[2 q + 1] =
 // cos(2 pi k / 2^23) evaluated directly (q < n).
 cudaError_t sg_launch_opinion_cos_check(const float2 *trig, int32_t k0, int32_t n, double *out, cudaStream_t st);
