@@ -396,9 +396,11 @@ int sg_server_set_tune(sg_server *s, const sg_tune *t);
  * RNG key = agent index. All scratch memory comes from one static device array
  * of SG_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until
  * exit; the call allocates nothing. n above SG_NOALLOC_MAX_AGENTS is rejected
- * with SG_ERR_INVALID (message via sg_last_error(NULL, ...)). The first call on
- * a device looks up the array's device address (cudaGetSymbolAddress) with
- * that device current; make that first call before any stream capture. Calls
+ * with SG_ERR_INVALID (message via sg_last_error(NULL, ...)). The first call in
+ * each CUDA context (the device's primary context, again after a device reset,
+ * or a context of the caller's own) looks up the array's device address
+ * (cudaGetSymbolAddress) with that context current; make that first call before
+ * any stream capture. Calls
  * share the array: calls that overlap on the GPU race and give wrong results;
  * calls on one stream are safe. Asynchronous on `stream` (NULL = legacy). */
 #define SG_NOALLOC_MAX_AGENTS 1048576
