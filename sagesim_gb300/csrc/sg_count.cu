@@ -238,16 +238,25 @@ __device__ __forceinline__ bool hybrid_loop_tick(const SgTickArgs &a)
 // single warp walks a hub's whole row; the chunk pass skips such rows.
 constexpr int32_t kSegRow = 256;
 
-__device__ __forceinline__ void publish_long_row(const SgTickArgs &a, int32_t g, int32_t delta)
+// What the scatter needs of changed agent g, whose change-list entry is
+// `slot`: a long transpose row goes to the segment list (its recorded row is
+// then empty); the row [begin, end) is recorded beside the entry when the
+// change-row array is kept, so the scatter does not load the offsets again.
+__device__ __forceinline__ void record_changed_row(const SgTickArgs &a, int32_t slot, int32_t g, int32_t delta)
 {
+    if (!a.change_rows && !a.rowsegs) return;
     const int32_t b = __ldg(a.toff + g), e = __ldg(a.toff + g + 1);
-    if (e - b <= kSegRow) return;
-    const int32_t nseg = (e - b + kSegRow - 1) / kSegRow;
-    const int32_t base = atomicAdd(a.nrowsegs + a.r, nseg);
-    for (int32_t j = 0; j < nseg; ++j) {
-        const int32_t sb = b + j * kSegRow;
-        a.rowsegs[base + j] = SgRowSeg{sb, min(sb + kSegRow, e), delta, 0};
+    int32_t re = e;
+    if (a.rowsegs && e - b > kSegRow) {
+        const int32_t nseg = (e - b + kSegRow - 1) / kSegRow;
+        const int32_t base = atomicAdd(a.nrowsegs + a.r, nseg);
+        for (int32_t j = 0; j < nseg; ++j) {
+            const int32_t sb = b + j * kSegRow;
+            a.rowsegs[base + j] = SgRowSeg{sb, min(sb + kSegRow, e), delta, 0};
+        }
+        re = b;
     }
+    if (a.change_rows) a.change_rows[slot] = make_int2(b, re);
 }
 
 // Count-strategy step. Late in an epidemic this is a streaming pass over every
@@ -435,9 +444,12 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickAr
                     int32_t pos = 0;
                     if (lane == leader) pos = atomicAdd(&nch, __popc(m));
                     pos = __shfl_sync(FULL_MASK, pos, leader);
-                    if (has) tchanges[pos + __popc(m & ((1u << lane) - 1u))] = code;
+                    if (has) {
+                        const int32_t slot = pos + __popc(m & ((1u << lane) - 1u));
+                        tchanges[slot] = code;
+                        record_changed_row(a, tile.begin + slot, i, code >= 0 ? 1 : -1);
+                    }
                 }
-                if (has && a.rowsegs) publish_long_row(a, i, code >= 0 ? 1 : -1);
             }
         }
         __syncthreads();
@@ -455,7 +467,8 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickAr
             __syncthreads();
             if (a.chunks && n > 0) {
                 const int32_t base = chunk_base;
-                for (int32_t j = tid; j < c; j += SG_SIR_THREADS) a.chunks[base + j] = SgChunk{t, j};
+                for (int32_t j = tid; j < c; j += SG_SIR_THREADS)
+                    a.chunks[base + j] = SgChunk{tile.begin + 32 * j, min(32, n - 32 * j)};
             }
         }
         if (STATS && a.segs[tile.seg].stats)
@@ -731,7 +744,6 @@ __global__ void __launch_bounds__(SG_SIR_THREADS, 4) sir_count_flat_kernel(SgTic
                     const bool rec = (imask >> e) & 1u;
                     state[i] = rec ? cr : ci;
                     if (a.cls) a.cls[i] = (uint8_t)(rec ? 2 : 1);
-                    if (a.rowsegs) publish_long_row(a, i, rec ? -1 : 1);
                 }
         }
         if (__any_sync(FULL_MASK, hits)) {
@@ -750,7 +762,10 @@ __global__ void __launch_bounds__(SG_SIR_THREADS, 4) sir_count_flat_kernel(SgTic
             for (int e = 0; e < kFlatPer; ++e)
                 if ((hits >> e) & 1u) {
                     const int32_t i = b0 + e;
-                    tchanges[pos++] = (imask >> e) & 1u ? ~i : i;
+                    const bool rec = (imask >> e) & 1u;
+                    tchanges[pos] = rec ? ~i : i;
+                    record_changed_row(a, tile.begin + pos, i, rec ? -1 : 1);
+                    ++pos;
                 }
         }
         if (STATS) {
@@ -782,7 +797,8 @@ __global__ void __launch_bounds__(SG_SIR_THREADS, 4) sir_count_flat_kernel(SgTic
             __syncthreads();
             if (a.chunks && n > 0) {
                 const int32_t base = chunk_base;
-                for (int32_t j = tid; j < c; j += SG_SIR_THREADS) a.chunks[base + j] = SgChunk{t, j};
+                for (int32_t j = tid; j < c; j += SG_SIR_THREADS)
+                    a.chunks[base + j] = SgChunk{tile.begin + 32 * j, min(32, n - 32 * j)};
             }
         }
         __syncthreads(); // shared memory is rewritten by the next tile
@@ -1052,7 +1068,7 @@ __global__ void __launch_bounds__(SG_SIR_THREADS, 5) sir_count_sweep_kernel(SgTi
                 a.cls[i] = (uint8_t)(infk[u] ? 2 : 1);
                 const int32_t p = atomicAdd(&sh_nch[tw[u] / WPT], 1);
                 a.changes[tp.begin + p] = infk[u] ? ~i : i;
-                if (a.rowsegs) publish_long_row(a, i, infk[u] ? -1 : 1);
+                record_changed_row(a, tp.begin + p, i, infk[u] ? -1 : 1);
                 if (STATS) {
                     // S -> I: S - 1, I + 1; I -> R: I - 1, R + 1 (sums mod 2^64)
                     atomicAdd(&sh_dstat[tw[u]][infk[u] ? 1 : 0], ~0ull);
@@ -1073,7 +1089,7 @@ __global__ void __launch_bounds__(SG_SIR_THREADS, 5) sir_count_sweep_kernel(SgTi
                 int32_t cb = 0;
                 if (lane == 0) cb = atomicAdd(a.nchunks + a.r, c);
                 cb = __shfl_sync(FULL_MASK, cb, 0);
-                for (int32_t j = lane; j < c; j += 32) a.chunks[cb + j] = SgChunk{t, j};
+                for (int32_t j = lane; j < c; j += 32) a.chunks[cb + j] = SgChunk{my.begin + 32 * j, min(32, n - 32 * j)};
             }
         }
         if (t < a.ntiles) {
@@ -1189,20 +1205,28 @@ __device__ __forceinline__ void scatter_rows_lb(const SgTickArgs &a, int32_t b, 
     }
 }
 
-// One warp's 32 changes of a tile (q0 = first, n = the tile's change count).
+// One warp's 32 changes (entries q0 .. q0 + 31 of the list at `first`, n in
+// all). With the change-row array the entry and its row are two independent
+// loads; without it the row's offsets are loaded after the entry.
 template <bool LB>
-__device__ __forceinline__ void scatter_changes(const SgTickArgs &a, const int32_t *tchanges, int32_t q0,
-                                                int32_t n, int lane, bool sb)
+__device__ __forceinline__ void scatter_changes(const SgTickArgs &a, int32_t first, int32_t q0, int32_t n, int lane,
+                                                bool sb)
 {
     const int32_t q = q0 + lane;
     const bool valid = q < n;
-    const int32_t c = valid ? tchanges[q] : 0;
-    const int32_t g = c >= 0 ? c : ~c;
+    const int32_t c = valid ? a.changes[first + q] : 0;
     const int32_t delta = c >= 0 ? 1 : -1;
     int32_t b = 0, e = 0;
     if (valid) {
-        b = __ldg(a.toff + g);
-        e = __ldg(a.toff + g + 1);
+        if (a.change_rows) {
+            const int2 row = a.change_rows[first + q];
+            b = row.x;
+            e = row.y;
+        } else {
+            const int32_t g = c >= 0 ? c : ~c;
+            b = __ldg(a.toff + g);
+            e = __ldg(a.toff + g + 1);
+        }
     }
     if (a.rowsegs && e - b > kSegRow) e = b; // handled through the row-segment list
     if (LB)
@@ -1241,8 +1265,7 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_scatter_chunks_kerne
     const bool sb = scatter_sets_bits(a);
     for (int32_t w = blockIdx.x * kWarps + warp; w < nck; w += gridDim.x * kWarps) {
         const SgChunk ck = a.chunks[w];
-        scatter_changes<LB>(a, a.changes + a.tiles[ck.tile].begin, ck.chunk * 32, __ldg(a.tile_nch + ck.tile),
-                            lane, sb);
+        scatter_changes<LB>(a, ck.first, 0, ck.count, lane, sb);
     }
     if (a.rowsegs) scatter_row_segments(a, lane, blockIdx.x * kWarps + warp, gridDim.x * kWarps, sb);
 }
@@ -1257,8 +1280,8 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_scatter_kernel(SgTic
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
         const int32_t n = a.tile_nch[t];
         if (n == 0) continue;
-        const int32_t *tchanges = a.changes + a.tiles[t].begin;
-        for (int32_t q0 = warp * 32; q0 < n; q0 += SG_SIR_THREADS) scatter_changes<LB>(a, tchanges, q0, n, lane, sb);
+        const int32_t first = a.tiles[t].begin;
+        for (int32_t q0 = warp * 32; q0 < n; q0 += SG_SIR_THREADS) scatter_changes<LB>(a, first, q0, n, lane, sb);
     }
     if (a.rowsegs) scatter_row_segments(a, lane, blockIdx.x * kWarps + warp, gridDim.x * kWarps, sb);
 }

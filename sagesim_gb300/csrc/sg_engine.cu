@@ -78,7 +78,7 @@ struct sg_engine {
     int32_t next_step_id = 0;
 
     // scratch of the count strategy and of per-tick statistics
-    SgDev cnt, changes, tile_nch, stats, chunks, nchunks, rowsegs, nrowsegs;
+    SgDev cnt, changes, change_rows, tile_nch, stats, chunks, nchunks, rowsegs, nrowsegs;
     SgDev cls, amask, mrebuild, tick_changes, tick_cand; // class sweep: classes, activity bits, per-tick counters
     bool cls_on = false;     // this run's count step keeps classes (its tiles start at multiples of 32)
     bool last_sweep = false; // the last run's count step was the class sweep
@@ -674,6 +674,7 @@ static SgTickArgs base_args(sg_engine *e, SgStep *s, int32_t r, bool inplace)
     if (e->cls_on && s->bp.strategy == SG_SIR_COUNT)
         a.cnt_window = std::min(e->l2_window_max, (size_t)e->n * sizeof(int32_t));
     a.changes = e->changes.as<int32_t>();
+    a.change_rows = s->bp.strategy == SG_SIR_COUNT ? e->change_rows.as<int2>() : nullptr;
     a.tile_nch = e->tile_nch.as<int32_t>();
     a.chunks = e->chunks.as<SgChunk>();
     a.nchunks = e->nchunks.as<int32_t>();
@@ -856,6 +857,7 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
         if (rc) return rc;
         SG_CK(e->cnt.reserve((size_t)std::max<int64_t>(e->n, 1) * 4));
         SG_CK(e->changes.reserve((size_t)std::max<int64_t>(e->n, 1) * 4));
+        SG_CK(e->change_rows.reserve((size_t)std::max<int64_t>(e->n, 1) * sizeof(int2)));
     }
     if (pl.frontier) {
         if (!pl.count_inplace)

@@ -90,9 +90,10 @@ inline int32_t sg_sweep_wpt(int64_t ntiles, int sm_count, int32_t flavour)
     return 4;
 }
 
-// One warp's share of the scatter: changes [32 * chunk, 32 * chunk + 32) of a tile.
+// One warp's share of the scatter: change-list entries [first, first + count),
+// count <= 32 (a tile's changes in runs of 32).
 struct SgChunk {
-    int32_t tile, chunk;
+    int32_t first, count;
 };
 
 // Part [begin, end) of a changed hub's transpose row, with the change's +-1.
@@ -119,6 +120,9 @@ struct SgTickArgs {
     int32_t *cnt;           // infected-neighbour count per agent
     int32_t *changes;       // change list: agent index, ~agent for I->R; tile t
                             // owns changes[tile.begin .. tile.begin + tile_nch[t])
+    int2 *change_rows;      // NULL, or beside each change-list entry the changed agent's
+                            // transpose row [begin, end) (end = begin when the row goes
+                            // through the long-row segments), so the scatter need not load it
     int32_t *tile_nch;      // [ntiles] changes recorded by each tile this tick
     SgChunk *chunks;        // NULL, or the scatter's work list of non-empty chunks
     int32_t *nchunks;       // [ticks] chunk counts, slot r (zero before the run)
