@@ -22,7 +22,8 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-Wall", "-I" + B
          "-I" + INCLUDE]
 SOURCES = ["sg_kernels.cu", "sg_count.cu", "sg_engine.cu", "sg_batch.cu", "sg_server.cpp", "sg_step_rt.cpp",
            "sg_graphs.cpp", "sg_noalloc.cu", "sg_setup.cu"]
-HEADERS = ["sg_kernels.h", "sg_device.cuh", "sg_setup.h", "sg_internal.h", "sg_philox.h", "sg_step_rt.h", "sg_batch.h"]
+HEADERS = ["sg_kernels.h", "sg_device.cuh", "sg_setup.h", "sg_internal.h", "sg_philox.h", "sg_step_rt.h", "sg_batch.h",
+           "sg_count_flat.cuh"]
 
 
 def _nvcc():

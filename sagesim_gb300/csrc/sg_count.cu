@@ -478,332 +478,7 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickAr
 }
 
 // ---- count step, flat draws (busy ticks) -----------------------------------------------
-// Near an epidemic's peak most agents draw: an infected agent one recovery draw
-// (salt 1), a susceptible agent with k infected neighbours k infection draws
-// (SIR-B: salt 2 .. 2+k-1; SIR-A: one, salt 1). Giving each thread a fixed set
-// of agents makes a warp run as long as its busiest lane. Here a block lays the
-// draws of its tile's candidates end to end (a block-wide scan of the
-// per-thread draw counts) and every thread evaluates an equal, contiguous
-// share of that sequence: it finds the owner of its first draw by a binary
-// search over the candidates' starts in shared memory and walks forward. The
-// draws of one candidate may be split between threads; all are evaluated (the
-// outcome depends only on whether some draw j < k is below beta, so no order
-// or early exit is needed). Hits are bits in shared memory. Draws beyond
-// kFlatCap of one candidate (hubs surrounded by infected agents) are done
-// afterwards, warp-wide, only for those candidates still without a hit. The
-// thread that owns an agent then applies its transition exactly as the loop
-// form does: state in place, class byte, change list, long-row segments.
-//
-// Thread tid owns the 8 consecutive agents tile.begin + 8 tid .. + 7, read as
-// one 8-byte class load (or two 16-byte state loads without class bytes) and
-// two 16-byte count loads; a warp's loads are 256 B / 1 KiB contiguous.
-constexpr int32_t kFlatCap = 32;
-constexpr int kFlatPer = SG_TILE / SG_SIR_THREADS;
-constexpr int kFlatIlp = 4; // draws a thread evaluates side by side
-static_assert(kFlatPer == 8, "the flat step gives each thread 8 agents of a tile");
-
-// U independent Philox streams at once (the same rounds as sg_philox_k23_keys):
-// the round chains of one draw are strictly sequential, so a thread keeps U of
-// them in flight to hide the multiply and xor latencies.
-template <int U>
-__device__ __forceinline__ void philox_k23_ilp(uint32_t (&c0)[U], uint32_t (&c1)[U], const SgPhiloxKeys &ks)
-{
-#pragma unroll
-    for (int r = 0; r < 10; ++r) {
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const uint64_t p = (uint64_t)c0[u] * SG_PHILOX_M;
-            c0[u] = (uint32_t)(p >> 32) ^ ks.k[r] ^ c1[u];
-            c1[u] = (uint32_t)p;
-        }
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u) c0[u] &= 0x7FFFFFu;
-}
-
-template <int VARIANT, bool STATS>
-__global__ void __launch_bounds__(SG_SIR_THREADS, 4) sir_count_flat_kernel(SgTickArgs a)
-{
-    if (a.hybrid_rise > 0) {
-        if (!hybrid_loop_tick(a)) return; // the class sweep takes this tick
-        // activity bits owed a rebuild stay owed until a sweep tick rebuilds them
-        if (blockIdx.x == 0 && threadIdx.x == 0 && a.mrebuild && a.mrebuild[a.r]) a.mrebuild[a.r + 1] = 1;
-    }
-    __shared__ int32_t sh_start[SG_TILE + 1]; // first draw of candidate c; [ncand] = the tile's draws
-    __shared__ uint32_t sh_lid[SG_TILE];      // RNG key of candidate c
-    __shared__ uint16_t sh_info[SG_TILE];     // slot of candidate c in the tile | 0x800 for a recovery
-    __shared__ uint32_t sh_hit[SG_TILE / 32]; // hit bit per slot
-    __shared__ unsigned long long sh_wtot[kWarps];
-    __shared__ unsigned long long red[4][kWarps];
-    __shared__ int32_t nch, chunk_base;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    int32_t cur_seg = -1;
-    int64_t tick = 0, end_tick = 0;
-    uint32_t c0b = 0, key = 0, kinf = 0, krec = 0;
-    int32_t cs = 0, ci = 0, cr = 0, lid_base = 0;
-    const uint32_t *lids = nullptr;
-    SgPhiloxKeys ks = sg_philox_keys(0);
-    int32_t *const state = (int32_t *)a.buf0; // updated in place
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-        const SgTile tile = a.tiles[t];
-        if (tile.seg != cur_seg) {
-            const SgSeg &sg = a.segs[tile.seg];
-            cur_seg = tile.seg;
-            tick = sg.tick0 + a.r;
-            end_tick = sg.end_tick;
-            c0b = sg_c0base(tick);
-            key = sg.key;
-            ks = sg_philox_keys(key);
-            kinf = sg.kinf;
-            krec = sg.krec;
-            cs = sg.cs;
-            ci = sg.ci;
-            cr = sg.cr;
-            lids = sg.lids;
-            lid_base = sg.lid_base;
-        }
-        if (tick >= end_tick) {
-            if (tid == 0) a.tile_nch[t] = 0;
-            continue;
-        }
-        const int32_t b0 = tile.begin + tid * kFlatPer;
-        const bool fast = b0 + kFlatPer <= tile.end && (b0 & 7) == 0; // whole, 32-byte aligned run
-        // 1. classes (byte e of cw: 0 S, 1 I, 2 R, 3 other or outside the tile),
-        //    counts and RNG keys of this thread's agents. In the aligned case the
-        //    three are independent loads issued together (one memory round trip);
-        //    counts and keys are needed by most agents of a busy tick anyway.
-        unsigned long long cw = 0x0303030303030303ull;
-        int32_t k[kFlatPer];
-        uint32_t l[kFlatPer];
-        if (fast) {
-            int4 c0, c1;
-            uint4 l0 = make_uint4(0, 0, 0, 0), l1 = l0;
-            if (a.cls) {
-                cw = *reinterpret_cast<const unsigned long long *>(a.cls + b0);
-            }
-            c0 = *reinterpret_cast<const int4 *>(a.cnt + b0);
-            c1 = *reinterpret_cast<const int4 *>(a.cnt + b0 + 4);
-            if (lids) {
-                l0 = __ldg(reinterpret_cast<const uint4 *>(lids + b0));
-                l1 = __ldg(reinterpret_cast<const uint4 *>(lids + b0 + 4));
-            }
-            if (!a.cls) {
-                const int4 v0 = *reinterpret_cast<const int4 *>(state + b0);
-                const int4 v1 = *reinterpret_cast<const int4 *>(state + b0 + 4);
-                const int32_t sv[kFlatPer] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
-                cw = 0;
-#pragma unroll
-                for (int e = 0; e < kFlatPer; ++e) {
-                    const unsigned long long c = sv[e] == ci ? 1u : sv[e] == cs ? 0u : sv[e] == cr ? 2u : 3u;
-                    cw |= c << (8 * e);
-                }
-            }
-            k[0] = c0.x, k[1] = c0.y, k[2] = c0.z, k[3] = c0.w, k[4] = c1.x, k[5] = c1.y, k[6] = c1.z, k[7] = c1.w;
-            if (lids) {
-                l[0] = l0.x, l[1] = l0.y, l[2] = l0.z, l[3] = l0.w, l[4] = l1.x, l[5] = l1.y, l[6] = l1.z, l[7] = l1.w;
-            } else {
-#pragma unroll
-                for (int e = 0; e < kFlatPer; ++e) l[e] = (uint32_t)(b0 + e - lid_base);
-            }
-        } else {
-#pragma unroll
-            for (int e = 0; e < kFlatPer; ++e) {
-                const int32_t i = b0 + e;
-                unsigned long long c = 3u;
-                if (i < tile.end) {
-                    if (a.cls) {
-                        c = a.cls[i];
-                    } else {
-                        const int32_t sv = state[i];
-                        c = sv == ci ? 1u : sv == cs ? 0u : sv == cr ? 2u : 3u;
-                    }
-                }
-                cw = (cw & ~(0xFFull << (8 * e))) | (c << (8 * e));
-                k[e] = c == 0u ? a.cnt[i] : 0;
-                l[e] = c <= 1u ? (lids ? __ldg(lids + i) : (uint32_t)(i - lid_base)) : 0u;
-            }
-        }
-        auto cls_of = [&](int e) -> uint32_t { return (uint32_t)(cw >> (8 * e)) & 0xFFu; };
-        // 2. draws per agent: a recovery draw per infected agent, min(k, kFlatCap)
-        //    infection draws (SIR-A: one) per susceptible agent with k > 0
-        uint32_t imask = 0, cand = 0, more = 0;
-        int32_t ndraw = 0;
-#pragma unroll
-        for (int e = 0; e < kFlatPer; ++e) {
-            const uint32_t c = cls_of(e);
-            if (c != 0u) k[e] = 0;
-            imask |= (uint32_t)(c == 1u) << e;
-            cand |= (uint32_t)(c == 1u || k[e] > 0) << e;
-            ndraw += c == 1u ? 1 : (VARIANT == 1 ? (k[e] > 0) : min(k[e], kFlatCap));
-            if (VARIANT == 2) more |= (uint32_t)(k[e] > kFlatCap) << e;
-        }
-        // 3. block-wide exclusive scan of (candidates << 32 | draws)
-        const unsigned long long mine = ((unsigned long long)__popc(cand) << 32) | (unsigned)ndraw;
-        unsigned long long x = mine;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned long long y = __shfl_up_sync(FULL_MASK, x, o);
-            if (lane >= o) x += y;
-        }
-        if (lane == 31) sh_wtot[warp] = x;
-        if (tid < SG_TILE / 32) sh_hit[tid] = 0u;
-        if (tid == 0) nch = 0;
-        __syncthreads();
-        unsigned long long before = 0, total = 0;
-#pragma unroll
-        for (int w = 0; w < kWarps; ++w) {
-            const unsigned long long v = sh_wtot[w];
-            before += w < warp ? v : 0ull;
-            total += v;
-        }
-        const int32_t ncand = (int32_t)(total >> 32), ntot = (int32_t)(total & 0xFFFFFFFFull);
-        {
-            const unsigned long long ex = before + x - mine;
-            int32_t cpos = (int32_t)(ex >> 32), dpos = (int32_t)(ex & 0xFFFFFFFFull);
-#pragma unroll
-            for (int e = 0; e < kFlatPer; ++e)
-                if ((cand >> e) & 1u) {
-                    const bool rec = (imask >> e) & 1u;
-                    sh_start[cpos] = dpos;
-                    sh_info[cpos] = (uint16_t)((tid * kFlatPer + e) | (rec ? 0x800 : 0));
-                    sh_lid[cpos] = l[e];
-                    ++cpos;
-                    dpos += rec || VARIANT == 1 ? 1 : min(k[e], kFlatCap);
-                }
-        }
-        if (tid == 0) sh_start[ncand] = ntot;
-        __syncthreads();
-        // 4. an equal share of the tile's draws per thread, kFlatIlp side by side
-        {
-            const int32_t per = (ntot + SG_SIR_THREADS - 1) / SG_SIR_THREADS;
-            int32_t d = tid * per;
-            const int32_t dend = min(d + per, ntot);
-            if (d < dend) {
-                int32_t lo = 0, hi = ncand - 1; // owner of draw d: the last c with sh_start[c] <= d
-                while (lo < hi) {
-                    const int32_t mid = (lo + hi + 1) >> 1;
-                    if (sh_start[mid] <= d) lo = mid;
-                    else hi = mid - 1;
-                }
-                int32_t c = lo;
-                int32_t cstart = sh_start[c], cend = sh_start[c + 1];
-                uint32_t info = sh_info[c], clid = sh_lid[c];
-                for (; d < dend; d += kFlatIlp) {
-                    uint32_t c0[kFlatIlp], c1[kFlatIlp], th[kFlatIlp], in[kFlatIlp];
-#pragma unroll
-                    for (int u = 0; u < kFlatIlp; ++u) {
-                        const int32_t dd = d + u;
-                        const bool valid = dd < dend;
-                        // every candidate has at least one draw, so consecutive
-                        // draws belong to the same candidate or to the next one
-                        if (valid && dd >= cend) {
-                            ++c;
-                            cstart = cend;
-                            cend = sh_start[c + 1];
-                            info = sh_info[c];
-                            clid = sh_lid[c];
-                        }
-                        const bool rec = (info & 0x800u) != 0;
-                        c0[u] = c0b + (rec || VARIANT == 1 ? 1u : 2u + (uint32_t)(dd - cstart));
-                        c1[u] = clid;
-                        th[u] = valid ? (rec ? krec : kinf) : 0u; // 0: never a hit
-                        in[u] = info;
-                    }
-                    philox_k23_ilp<kFlatIlp>(c0, c1, ks);
-#pragma unroll
-                    for (int u = 0; u < kFlatIlp; ++u)
-                        if (c0[u] < th[u]) atomicOr(&sh_hit[(in[u] & 0x7FFu) >> 5], 1u << (in[u] & 31u));
-                }
-            }
-        }
-        __syncthreads();
-        uint32_t hits = (sh_hit[tid >> 2] >> ((tid & 3) * kFlatPer)) & 0xFFu;
-        // 5. draws kFlatCap .. k-1 of susceptible agents that need more, warp-wide
-        if (VARIANT == 2 && __any_sync(FULL_MASK, more & ~hits)) {
-#pragma unroll
-            for (int e = 0; e < kFlatPer; ++e) {
-                unsigned m = __ballot_sync(FULL_MASK, ((more & ~hits) >> e) & 1u);
-                while (m) {
-                    const int src = __ffs(m) - 1;
-                    m &= m - 1;
-                    const int32_t bk = __shfl_sync(FULL_MASK, k[e], src);
-                    const uint32_t bl = __shfl_sync(FULL_MASK, l[e], src);
-                    const bool h = warp_draws((uint32_t)kFlatCap, bk - kFlatCap, c0b, bl, key, kinf, lane);
-                    if (lane == src && h) hits |= 1u << e;
-                }
-            }
-        }
-        // 6. transitions: state in place, class byte, long rows, then the change
-        //    list (one shared-memory atomic per warp with changes)
-        int32_t *tchanges = a.changes + tile.begin;
-        if (hits) {
-#pragma unroll
-            for (int e = 0; e < kFlatPer; ++e)
-                if ((hits >> e) & 1u) {
-                    const int32_t i = b0 + e;
-                    const bool rec = (imask >> e) & 1u;
-                    state[i] = rec ? cr : ci;
-                    if (a.cls) a.cls[i] = (uint8_t)(rec ? 2 : 1);
-                }
-        }
-        if (__any_sync(FULL_MASK, hits)) {
-            const int32_t nh = __popc(hits);
-            int32_t incl = nh;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int32_t y = __shfl_up_sync(FULL_MASK, incl, o);
-                if (lane >= o) incl += y;
-            }
-            int32_t base = 0;
-            if (lane == 31) base = atomicAdd(&nch, incl);
-            base = __shfl_sync(FULL_MASK, base, 31);
-            int32_t pos = base + incl - nh;
-#pragma unroll
-            for (int e = 0; e < kFlatPer; ++e)
-                if ((hits >> e) & 1u) {
-                    const int32_t i = b0 + e;
-                    const bool rec = (imask >> e) & 1u;
-                    tchanges[pos] = rec ? ~i : i;
-                    record_changed_row(a, tile.begin + pos, i, rec ? -1 : 1);
-                    ++pos;
-                }
-        }
-        if (STATS) {
-            unsigned long long nS = 0, nI = 0, nR = 0, eS = 0;
-#pragma unroll
-            for (int e = 0; e < kFlatPer; ++e) {
-                const int32_t i = b0 + e;
-                const uint32_t c = cls_of(e);
-                if (c == 0u) eS += (unsigned long long)(__ldg(a.off + i + 1) - __ldg(a.off + i));
-                const uint32_t after = (hits >> e) & 1u ? ((imask >> e) & 1u ? 2u : 1u) : c;
-                nS += after == 0u;
-                nI += after == 1u;
-                nR += after == 2u;
-            }
-            if (a.segs[tile.seg].stats)
-                block_flush4(nS, nI, nR, eS, a.segs[tile.seg].stats + 4 * (int64_t)a.r, red);
-        }
-        __syncthreads();
-        {
-            // the tile's change count and its 32-change chunks for the scatter
-            const int32_t n = nch;
-            const int32_t c = (n + 31) >> 5;
-            if (tid == 0) {
-                a.tile_nch[t] = n;
-                if (a.tick_changes && n > 0) atomicAdd(a.tick_changes + a.r, n);
-                if (a.tick_cand) atomicAdd(a.tick_cand + a.r, tile.end - tile.begin);
-                if (a.chunks && n > 0) chunk_base = atomicAdd(a.nchunks + a.r, c);
-            }
-            __syncthreads();
-            if (a.chunks && n > 0) {
-                const int32_t base = chunk_base;
-                for (int32_t j = tid; j < c; j += SG_SIR_THREADS)
-                    a.chunks[base + j] = SgChunk{tile.begin + 32 * j, min(32, n - 32 * j)};
-            }
-        }
-        __syncthreads(); // shared memory is rewritten by the next tile
-    }
-}
+#include "sg_count_flat.cuh"
 
 // ---- count step, class sweep ---------------------------------------------------------
 // In-place count step over one-byte agent classes (a.cls: 0 S, 1 I, 2 R,
@@ -1374,8 +1049,15 @@ cudaError_t sg_launch_sir_count_step(const SgTickArgs &args, int variant, bool s
         if (nlaunched) *nlaunched = 2;
         // hybrid: the busy-tick form too (it returns at once in sweep ticks)
     }
-    if ((a.flavour & SG_FLAVOUR_FLAT) && inplace) {
-        // flat draws take the busy ticks (or every tick without the hybrid)
+    if ((a.flavour & SG_FLAVOUR_FLAT) && inplace && a.chunks) {
+        // flat draws take the busy ticks (or every tick without the hybrid); two
+        // blocks per resident slot balance tiles of unequal cost better than
+        // one wave of many-tile blocks or a block per tile
+        int dev = 0, sms = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+            return cudaErrorInvalidDevice;
+        grid = std::max(1, std::min(grid, 2 * kFlatBlocksPerSm * sms));
         if (variant == 1) {
             if (stats) launch_count_kernel(sir_count_flat_kernel<1, true>, a, grid, st);
             else launch_count_kernel(sir_count_flat_kernel<1, false>, a, grid, st);
