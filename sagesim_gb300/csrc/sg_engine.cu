@@ -86,7 +86,7 @@ struct sg_engine {
     SgDev transpose_tmp, scan_tmp;
     SgDev bm_radius, bm_trig; // opinion: Box-Muller tables, built once per engine
     bool bm_ready = false;
-    SgDev nb8;               // opinion (width 8): first 8 neighbours per agent, column-major, -1 padded
+    SgDev nb8;               // opinion (width 8): first 8 neighbours per agent, group-major, -1 padded
     bool nb8_valid = false;  // nb8 matches the current graph
     bool l2_limit_set = false;
     SgDev prop_table; // sg_prop_dev per property, for compiled steps
@@ -797,7 +797,6 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
                 a.bm_radius = e->bm_ready ? e->bm_radius.as<float2>() : nullptr;
                 a.bm_trig = e->bm_ready ? e->bm_trig.as<float2>() : nullptr;
                 a.nb8 = e->nb8_valid && s->host_seg.width == 8 ? e->nb8.as<int32_t>() : nullptr;
-                a.nb8_stride = e->n;
                 {
                     const double sg = s->bp.sigma;
                     a.sigma_hi = (float)sg;
@@ -901,7 +900,7 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
         }
         if (s->kind == SG_BUILTIN_OPINION && s->host_seg.width == 8 && !e->nb8_valid && e->n > 0) {
             // the neighbour table of the width-8 opinion step, rebuilt with the graph
-            SG_CK(e->nb8.reserve((size_t)e->n * 8 * sizeof(int32_t)));
+            SG_CK(e->nb8.reserve((size_t)SG_NB8_ENTRIES(e->n) * sizeof(int32_t)));
             SG_CK(sg_launch_opinion_neighbours8(e->off.as<int32_t>(), e->idx.as<int32_t>(), e->n,
                                                 e->nb8.as<int32_t>(), e->stream));
             e->nb8_valid = true;

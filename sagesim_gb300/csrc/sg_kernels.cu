@@ -483,15 +483,20 @@ __global__ void opinion_tables_kernel(float2 *__restrict__ radius, float2 *__res
     }
 }
 
-// First 8 neighbours of every agent, column-major, -1 after the row ends.
+// First 8 neighbours of every agent, group-major (SG_NB8_AT), -1 after the row
+// ends and for the agents >= n of the last group.
 __global__ void opinion_neighbours8_kernel(const int32_t *__restrict__ off, const int32_t *__restrict__ idx,
                                            int64_t n, int32_t *__restrict__ nb8)
 {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t b = off[i];
-        const int32_t m = min(off[i + 1] - b, 8);
+    const int64_t nall = (n + 31) & ~(int64_t)31;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nall; i += (int64_t)gridDim.x * blockDim.x) {
+        int32_t b = 0, m = 0;
+        if (i < n) {
+            b = off[i];
+            m = min(off[i + 1] - b, 8);
+        }
 #pragma unroll
-        for (int j = 0; j < 8; ++j) nb8[j * n + i] = j < m ? idx[b + j] : -1;
+        for (int j = 0; j < 8; ++j) nb8[SG_NB8_AT(i, j)] = j < m ? idx[b + j] : -1;
     }
 }
 
@@ -641,7 +646,7 @@ __global__ void __launch_bounds__(kOpinionThreads, W == 8 ? 2 : 3) opinion_kerne
         }
         // 2. weights (read once per tick: evict-first loads keep L2 for the
         //    opinions, which neighbours re-read), own opinions, and the first 8
-        //    neighbours from the column-major table (each load instruction of a
+        //    neighbours from the group-major table (each load instruction of a
         //    warp is one 128-byte line)
         int32_t m[U], nb[U][8];
         float wv[U][8], xo[U];
@@ -653,7 +658,7 @@ __global__ void __launch_bounds__(kOpinionThreads, W == 8 ? 2 : 3) opinion_kerne
             wv[u][4] = w1.x, wv[u][5] = w1.y, wv[u][6] = w1.z, wv[u][7] = w1.w;
             xo[u] = xin[iu[u]];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) nb[u][j] = __ldcs(a.nb8 + j * a.nb8_stride + iu[u]);
+            for (int j = 0; j < 8; ++j) nb[u][j] = __ldcs(a.nb8 + SG_NB8_AT(iu[u], j));
         }
         // 3. the row length is the count of valid entries (they come first)
 #pragma unroll

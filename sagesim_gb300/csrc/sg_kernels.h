@@ -150,8 +150,8 @@ struct SgTickArgs {
     const float2 *bm_radius; // opinion: NULL, or the 2^23-entry Box-Muller radius table and
     const float2 *bm_trig;   // the split cosine tables of sg_launch_opinion_tables
     float sigma_hi, sigma_lo; // opinion: the noise sigma as a double-float pair (with the tables)
-    const int32_t *nb8;     // opinion, width 8: NULL, or nb8[j * nb8_stride + i] = the j-th
-    int64_t nb8_stride;     // neighbour of agent i for j < min(deg, 8), -1 after (column-major)
+    const int32_t *nb8;     // opinion, width 8: NULL, or the neighbour table of
+                            // sg_launch_opinion_neighbours8 (SG_NB8_AT)
     const void *l2_win;     // opinion: NULL, or an access-policy window (persisting lines)
     size_t l2_win_bytes;    // over l2_win_bytes from l2_win, a fraction l2_win_hit of its
     float l2_win_hit;       // lines kept (the radius table, read at random)
@@ -203,9 +203,16 @@ cudaError_t sg_launch_opinion(const SgTickArgs &a, int grid, cudaStream_t st, in
 #define SG_BOX_MULLER_SIZE (1 << 23)
 #define SG_BM_TRIG_ENTRIES (4096 + 2 * 2048)
 cudaError_t sg_launch_opinion_tables(float2 *radius, float2 *trig, cudaStream_t st);
-// nb8[j * n + i] = indices[offsets[i] + j] for j < min(deg(i), 8), else -1: the
-// width-8 opinion step's neighbours in a column-major table, so that a warp's
-// loads of the j-th neighbours of 32 consecutive agents are one 128-byte line.
+// nb8[SG_NB8_AT(i, j)] = indices[offsets[i] + j] for j < min(deg(i), 8), else
+// -1: the width-8 opinion step's neighbours, group-major. Agents come in groups
+// of 32 (agent i in group i / 32), each group's table is 256 entries (1 KiB):
+// its agents' first neighbours, then their second neighbours, and so on. A
+// warp's loads of the j-th neighbours of 32 consecutive agents are one 128-byte
+// line, and the table of 32 consecutive groups is one contiguous 32 KiB range.
+// The table holds SG_NB8_ENTRIES(n) entries (whole groups; the entries of
+// agents >= n are -1).
+#define SG_NB8_AT(i, j) ((((int64_t)(i) >> 5) << 8) + ((int64_t)(j) << 5) + ((i) & 31))
+#define SG_NB8_ENTRIES(n) ((((int64_t)(n) + 31) >> 5) << 8)
 cudaError_t sg_launch_opinion_neighbours8(const int32_t *offsets, const int32_t *indices, int64_t n, int32_t *nb8,
                                           cudaStream_t st);
 // out[2 q] = the split-table cosine of k = k0 + q (hi + lo), out[2 q + 1] =
