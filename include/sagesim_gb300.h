@@ -276,6 +276,17 @@ int sg_profile_get(sg_engine *e, int32_t kind, char *name, size_t cap, int64_t *
  * method; no counterpart in the reference. */
 int sg_opinion_cosine_check(sg_engine *e, int32_t k0, int32_t n, double *split, double *direct);
 
+/* The opinion step's noise term for n host triples (opinion x[q], the normal
+ * draw's 23-bit integers k1[q], k2[q] < 2^23) at noise level sigma:
+ * out[q] = clamp(float32(x + sigma * sqrt(-2 log(k1 / 2^23 + 1e-10)) *
+ * cos(2 pi k2 / 2^23)), 0, 1) exactly as the step forms it (fixed-point radius,
+ * the pair table where the rounding is open), exact[q] = the same with the
+ * pair-table radius always, slow[q] = 1 where the pair table was needed. A
+ * check of the engine's own table method; no counterpart in the reference.
+ * SG_ERR_INVALID for a k outside [0, 2^23) or NULL arrays with n > 0. */
+int sg_opinion_noise_check(sg_engine *e, double sigma, int64_t n, const float *x, const uint32_t *k1,
+                           const uint32_t *k2, float *out, float *exact, uint8_t *slow);
+
 /* ---- ensembles: many independent SIR scenarios in one launch per tick ---------------
  * No single counterpart in the reference, which runs one model per process
  * (sagesim/model.py:961-998); each scenario here is what one reference Model

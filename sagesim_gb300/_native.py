@@ -135,6 +135,7 @@ SIGNATURES = {
     "sg_profile_enable": [_P, _I32],
     "sg_profile_get": [_P, _I32, ctypes.c_char_p, _SZ, ctypes.POINTER(_I64), ctypes.POINTER(_D)],
     "sg_opinion_cosine_check": [_P, _I32, _I32, _P, _P],
+    "sg_opinion_noise_check": [_P, _D, _I64, _P, _P, _P, _P, _P, _P],
     "sg_batch_create": [ctypes.POINTER(EngineCfg), ctypes.POINTER(_P)],
     "sg_batch_destroy": [_P],
     "sg_batch_last_error": [_P, ctypes.c_char_p, _SZ],

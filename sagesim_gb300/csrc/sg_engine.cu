@@ -84,7 +84,7 @@ struct sg_engine {
     bool last_sweep = false; // the last run's count step was the class sweep
     SgDev flist[2], flen, fnch, fmark, fstats_init, fstats_delta; // frontier strategy
     SgDev transpose_tmp, scan_tmp;
-    SgDev bm_radius, bm_trig; // opinion: Box-Muller tables, built once per engine
+    SgDev bm_radius, bm_rq, bm_trig; // opinion: Box-Muller tables, built once per engine
     bool bm_ready = false;
     SgDev nb8;               // opinion (width 8): first 8 neighbours per agent, group-major, -1 padded
     bool nb8_valid = false;  // nb8 matches the current graph
@@ -795,6 +795,7 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
                 }
             } else if (s->kind == SG_BUILTIN_OPINION) {
                 a.bm_radius = e->bm_ready ? e->bm_radius.as<float2>() : nullptr;
+                a.bm_rq = e->bm_ready ? e->bm_rq.as<uint32_t>() : nullptr;
                 a.bm_trig = e->bm_ready ? e->bm_trig.as<float2>() : nullptr;
                 a.nb8 = e->nb8_valid && s->host_seg.width == 8 ? e->nb8.as<int32_t>() : nullptr;
                 {
@@ -803,8 +804,8 @@ static int enqueue_ticks(sg_engine *e, const SgPlan &pl, int32_t nticks, bool st
                     a.sigma_lo = (float)(sg - (double)a.sigma_hi);
                 }
                 if (e->bm_ready && e->l2_limit_bytes) {
-                    a.l2_win = a.bm_radius;
-                    a.l2_win_bytes = std::min(e->l2_window_max, (size_t)SG_BOX_MULLER_SIZE * sizeof(float2));
+                    a.l2_win = a.bm_rq;
+                    a.l2_win_bytes = std::min(e->l2_window_max, SG_BM_RQ_BYTES);
                     a.l2_win_hit = (float)std::min(1.0, (double)e->l2_limit_bytes / (double)a.l2_win_bytes);
                 }
                 SG_PROF_LAUNCH("opinion", sg_launch_opinion(a, grid, e->stream, s->host_seg.width));
@@ -894,8 +895,10 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
         if (rc) return rc;
         if (s->kind == SG_BUILTIN_OPINION && !e->bm_ready) { // before any capture
             SG_CK(e->bm_radius.reserve((size_t)SG_BOX_MULLER_SIZE * sizeof(float2)));
+            SG_CK(e->bm_rq.reserve(SG_BM_RQ_BYTES));
             SG_CK(e->bm_trig.reserve((size_t)SG_BM_TRIG_ENTRIES * sizeof(float2)));
-            SG_CK(sg_launch_opinion_tables(e->bm_radius.as<float2>(), e->bm_trig.as<float2>(), e->stream));
+            SG_CK(sg_launch_opinion_tables(e->bm_radius.as<float2>(), e->bm_rq.as<uint32_t>(),
+                                           e->bm_trig.as<float2>(), e->stream));
             e->bm_ready = true;
         }
         if (s->kind == SG_BUILTIN_OPINION && s->host_seg.width == 8 && !e->nb8_valid && e->n > 0) {
@@ -932,8 +935,8 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
         e->l2_limit_set = true;
     }
     if (e->bm_ready && e->l2_window_max && !e->l2_limit_set) {
-        // the opinion step's radius table (64 MiB, read at random) as persisting lines
-        e->l2_limit_bytes = std::min(e->l2_window_max, (size_t)SG_BOX_MULLER_SIZE * sizeof(float2));
+        // the opinion step's radius corrections (32 MiB, read at random) as persisting lines
+        e->l2_limit_bytes = std::min(e->l2_window_max, SG_BM_RQ_BYTES);
         cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, e->l2_limit_bytes);
         (void)cudaGetLastError();
         e->l2_limit_set = true;
@@ -1190,7 +1193,7 @@ int sg_opinion_cosine_check(sg_engine *e, int32_t k0, int32_t n, double *split, 
     SgDev trig, out;
     SG_CK(trig.reserve((size_t)SG_BM_TRIG_ENTRIES * sizeof(float2)));
     SG_CK(out.reserve((size_t)n * 2 * sizeof(double)));
-    SG_CK(sg_launch_opinion_tables(nullptr, trig.as<float2>(), e->stream));
+    SG_CK(sg_launch_opinion_tables(nullptr, nullptr, trig.as<float2>(), e->stream));
     SG_CK(sg_launch_opinion_cos_check(trig.as<float2>(), k0, n, out.as<double>(), e->stream));
     std::vector<double> h((size_t)n * 2);
     SG_CK(cudaMemcpyAsync(h.data(), out.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
@@ -1199,6 +1202,44 @@ int sg_opinion_cosine_check(sg_engine *e, int32_t k0, int32_t n, double *split, 
         split[q] = h[2 * (size_t)q];
         direct[q] = h[2 * (size_t)q + 1];
     }
+    return SG_OK;
+}
+
+int sg_opinion_noise_check(sg_engine *e, double sigma, int64_t n, const float *x, const uint32_t *k1,
+                           const uint32_t *k2, float *out, float *exact, uint8_t *slow)
+{
+    if (!e || n < 0 || (n > 0 && (!x || !k1 || !k2 || !out || !exact || !slow))) return SG_ERR_INVALID;
+    for (int64_t q = 0; q < n; ++q)
+        if (k1[q] >= (uint32_t)SG_BOX_MULLER_SIZE || k2[q] >= (uint32_t)SG_BOX_MULLER_SIZE) return SG_ERR_INVALID;
+    if (n == 0) return SG_OK;
+    cudaSetDevice(e->device);
+    SgDev radius, rq, trig, dx, dk1, dk2, dout, dexact, dslow;
+    SG_CK(radius.reserve((size_t)SG_BOX_MULLER_SIZE * sizeof(float2)));
+    SG_CK(rq.reserve(SG_BM_RQ_BYTES));
+    SG_CK(trig.reserve((size_t)SG_BM_TRIG_ENTRIES * sizeof(float2)));
+    const size_t b4 = (size_t)n * 4;
+    SG_CK(dx.reserve(b4));
+    SG_CK(dk1.reserve(b4));
+    SG_CK(dk2.reserve(b4));
+    SG_CK(dout.reserve(b4));
+    SG_CK(dexact.reserve(b4));
+    SG_CK(dslow.reserve((size_t)n));
+    SG_CK(sg_launch_opinion_tables(radius.as<float2>(), rq.as<uint32_t>(), trig.as<float2>(), e->stream));
+    SG_CK(cudaMemcpyAsync(dx.p, x, b4, cudaMemcpyHostToDevice, e->stream));
+    SG_CK(cudaMemcpyAsync(dk1.p, k1, b4, cudaMemcpyHostToDevice, e->stream));
+    SG_CK(cudaMemcpyAsync(dk2.p, k2, b4, cudaMemcpyHostToDevice, e->stream));
+    SgTickArgs a{};
+    a.bm_radius = radius.as<float2>();
+    a.bm_rq = rq.as<uint32_t>();
+    a.bm_trig = trig.as<float2>();
+    a.sigma_hi = (float)sigma;
+    a.sigma_lo = (float)(sigma - (double)a.sigma_hi);
+    SG_CK(sg_launch_opinion_noise_check(a, dx.as<float>(), dk1.as<uint32_t>(), dk2.as<uint32_t>(), n,
+                                        dout.as<float>(), dexact.as<float>(), (uint8_t *)dslow.p, e->stream));
+    SG_CK(cudaMemcpyAsync(out, dout.p, b4, cudaMemcpyDeviceToHost, e->stream));
+    SG_CK(cudaMemcpyAsync(exact, dexact.p, b4, cudaMemcpyDeviceToHost, e->stream));
+    SG_CK(cudaMemcpyAsync(slow, dslow.p, (size_t)n, cudaMemcpyDeviceToHost, e->stream));
+    SG_CK(cudaStreamSynchronize(e->stream));
     return SG_OK;
 }
 

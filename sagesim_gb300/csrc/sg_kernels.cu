@@ -375,8 +375,12 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) frontier_scatter_kernel(SgTick
 // (sagesim/math_utils.py:231-255: u1 salt 1, u2 salt 1 + 73856093, +1e-10
 // guard). u1 and u2 are k / 2^23 for 23-bit Philox integers k.
 //  - radius sqrt(-2 log(u1 + 1e-10)) takes 2^23 values: it is evaluated once
-//    per engine in double (opinion_tables_kernel) and tabulated (64 MiB, kept
-//    in L2 as persisting lines);
+//    per engine in double (opinion_tables_kernel) and tabulated twice: as the
+//    correction to a float32 estimate the step recomputes (bm_radius_estimate;
+//    the difference in 32-bit fixed point, steps of 2^-40: 32 MiB, kept in L2
+//    as persisting lines, one 4-byte read per agent) and as double-float
+//    pairs (64 MiB, in DRAM; read only for results whose rounding the first
+//    form leaves open, see opinion_noise_try);
 //  - cos(2 pi u2) by the angle-addition formula cos(A + B) = cos A cos B -
 //    sin A sin B with k = 2048 kh + kl, A = 2 pi kh / 2^12, B = 2 pi kl / 2^23:
 //    cos A from a 4096-entry table (sin A is the same table a quarter turn
@@ -395,6 +399,22 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) frontier_scatter_kernel(SgTick
 // (A float32 Box-Muller was tried and rejected: opinions near the clamp at 0
 // differ by up to 1.5e-4 relative.)
 constexpr int32_t kBoxMullerSize = 1 << 23;
+constexpr double kRadiusStep = 1099511627776.0; // 2^40: steps of the radius correction per unit
+
+// A float32 estimate of the radius of the 23-bit integer k: sqrt(-2 ln(2)
+// log2(k 2^-23 + 1e-10)) with the hardware's approximate base-2 logarithm and a
+// correctly rounded square root, clamped at 0. Each operation is an explicitly
+// rounded intrinsic or that logarithm, so every kernel computes the same value
+// and the table's correction is the one for the step's estimate. The error is
+// largest near k = 2^23, where -log u is tiny and the logarithm's absolute
+// error (about 2^-22) dominates: up to the square root of that, about 2^-10.5;
+// far smaller elsewhere. The corrections' range (2^-9) covers it.
+__device__ __forceinline__ float bm_radius_estimate(uint32_t k)
+{
+    const float u = __fadd_rn(__fmul_rn(__uint2float_rn(k), 0x1p-23f), 1e-10f);
+    const float l = __fmul_rn(-1.38629436f, __log2f(u)); // -2 ln(2) log2(u)
+    return __fsqrt_rn(fmaxf(l, 0.0f));
+}
 constexpr int32_t kTrigA = 4096, kTrigB = 2048; // entries of the A (cos) and B (cos, sin) tables
 static_assert(kTrigA + 2 * kTrigB == SG_BM_TRIG_ENTRIES, "table layout");
 
@@ -463,12 +483,20 @@ __device__ __forceinline__ float2 bm_cos_split(const float2 *trig, uint32_t k)
     return ff_add(ff_mul(ca, cb), make_float2(-p.x, -p.y));
 }
 
-__global__ void opinion_tables_kernel(float2 *__restrict__ radius, float2 *__restrict__ trig)
+__global__ void opinion_tables_kernel(float2 *__restrict__ radius, uint32_t *__restrict__ rq,
+                                      float2 *__restrict__ trig)
 {
     const int32_t stride = gridDim.x * blockDim.x;
     const int32_t end = radius ? kBoxMullerSize : kTrigA; // radius NULL: the cosine tables only
     for (int32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < end; k += stride) {
-        if (radius) radius[k] = ff_split(bm_radius((uint32_t)k));
+        if (radius) {
+            const double rv = bm_radius((uint32_t)k);
+            radius[k] = ff_split(rv);
+            if (rq) { // the difference (exact in double) in steps of 2^-40
+                const double d = rv - (double)bm_radius_estimate((uint32_t)k);
+                rq[k] = (uint32_t)__double2int_rn(d * kRadiusStep);
+            }
+        }
         if (k < kTrigA) { // A = pi * k / 2^11
             double sv, cv;
             sincospi((double)k / 2048.0, &sv, &cv);
@@ -573,24 +601,85 @@ __device__ __forceinline__ float opinion_mean(const SgTickArgs &a, const SgSeg &
 // radius load, which need no graph data, go first.
 constexpr int kOpinionThreads = 512;
 
-// Noise and clamp for one agent: y = x + sigma * radius * cos, rounded to
-// float32 and clamped to [0, 1]. Rounding is monotone and keeps 0 and 1, so
-// clamping after rounding gives the same value as clamping first; a negative
-// value rounds to a non-positive float, stored as +0.
-__device__ __forceinline__ float opinion_noise(const SgTickArgs &a, const SgSeg &sg, const float2 *trig, float x,
-                                               float2 r, uint32_t k1, uint32_t k2)
+// Noise and clamp: y = x + sigma * radius * cos, rounded to float32 and
+// clamped to [0, 1]. Rounding is monotone and keeps 0 and 1, so clamping after
+// rounding gives the same value as clamping first; a negative value rounds to a
+// non-positive float, stored as +0.
+__device__ __forceinline__ float clamp_opinion(float y)
 {
-    float yf;
-    if (a.bm_radius && trig) {
+    return y <= 0.0f ? 0.0f : (y > 1.0f ? 1.0f : y);
+}
+
+// With the tables: x + sigma * r * c in double-float (r, c the radius and
+// cosine pairs), rounded to float32 and clamped.
+__device__ __forceinline__ float opinion_noise_pair(const SgTickArgs &a, float x, float2 r, float2 c)
+{
+    const float2 t = ff_mul(make_float2(a.sigma_hi, a.sigma_lo), ff_mul(r, c));
+    const float2 s2 = ff_two_sum(x, t.x); // x + t, rounded once
+    return clamp_opinion(ff_norm(s2.x, __fadd_rn(s2.y, t.y)).x);
+}
+
+// The same result from the estimate re of the radius of k1 and its correction
+// dq (steps of 2^-40), when it can tell: y is formed as in opinion_noise_pair
+// with r = re + dq 2^-40 (within 2^-41 of the double radius and 2^-40.9 of
+// the pair table's), and it differs from the pair-table value by at most E =
+// sigma |c| 2^-40 + 2^-42 (|t| + |y|) (that radius difference times sigma |c|,
+// plus both paths' double-float roundings, each a few 2^-48 of |t| and |y|).
+// When y - E and y + E round and clamp to the same float32, so does the
+// pair-table value (rounding is monotone). Otherwise (near a float32 rounding
+// boundary: about one draw in 10^5, most at tiny opinions, whose float32 steps
+// are finest) *sure is false.
+__device__ __forceinline__ float opinion_noise_try(const SgTickArgs &a, float x, float re, uint32_t dq, float2 c,
+                                                   bool *sure)
+{
+    // re + dq 2^-40 as a pair: dq's bits above the low 8 and its low 8 convert exactly
+    const float2 rh = ff_norm(re, __fmul_rn(__int2float_rn((int32_t)(dq & 0xFFFFFF00u)), 0x1p-40f));
+    const float2 r = ff_norm(rh.x, __fadd_rn(rh.y, __fmul_rn(__uint2float_rn(dq & 0xFFu), 0x1p-40f)));
+    const float2 t = ff_mul(make_float2(a.sigma_hi, a.sigma_lo), ff_mul(r, c));
+    const float2 s2 = ff_two_sum(x, t.x);
+    const float lo = __fadd_rn(s2.y, t.y);
+    const float e = __fmul_rn(__fadd_rn(__fadd_rn(fabsf(t.x), fabsf(s2.x)), 4.0f * a.sigma_hi * fabsf(c.x)), 0x1p-42f);
+    const float ya = clamp_opinion(__fadd_rn(s2.x, __fsub_rd(lo, e)));
+    const float yb = clamp_opinion(__fadd_rn(s2.x, __fadd_ru(lo, e)));
+    *sure = ya == yb;
+    return ya;
+}
+
+// Noise and clamp for one agent (k1, k2 the draw's two integers, dq the radius
+// correction of k1 when the tables are present): always the value of
+// opinion_noise_pair with the pair-table radius, which is read only when the
+// estimate and correction leave the rounding open. Without tables (no cosine
+// pairs) the expression is evaluated in double.
+__device__ __forceinline__ float opinion_noise(const SgTickArgs &a, const SgSeg &sg, const float2 *trig, float x,
+                                               uint32_t dq, uint32_t k1, uint32_t k2)
+{
+    if (a.bm_rq && a.bm_radius && trig) {
         const float2 c = bm_cos_split(trig, k2);
-        const float2 t = ff_mul(make_float2(a.sigma_hi, a.sigma_lo), ff_mul(r, c));
-        const float2 s2 = ff_two_sum(x, t.x); // x + t, rounded once
-        yf = ff_norm(s2.x, __fadd_rn(s2.y, t.y)).x;
-    } else {
-        const double z = __dmul_rn(bm_radius(k1), bm_cos(k2));
-        yf = __double2float_rn(__dadd_rn((double)x, __dmul_rn(sg.sigma, z)));
+        bool sure;
+        const float y = opinion_noise_try(a, x, bm_radius_estimate(k1), dq, c, &sure);
+        return sure ? y : opinion_noise_pair(a, x, __ldg(a.bm_radius + k1), c);
     }
-    return yf <= 0.0f ? 0.0f : (yf > 1.0f ? 1.0f : yf);
+    const double z = __dmul_rn(bm_radius(k1), bm_cos(k2));
+    return clamp_opinion(__double2float_rn(__dadd_rn((double)x, __dmul_rn(sg.sigma, z))));
+}
+
+// out[q] = the step's noise result for opinion x[q] and the draw's integers
+// k1[q], k2[q] (a.bm_radius, a.bm_rq, a.bm_trig and sigma set); exact[q] = the
+// value with the pair-table radius; slow[q] = 1 where the fixed-point radius
+// left the rounding open (q < n).
+__global__ void opinion_noise_check_kernel(SgTickArgs a, const float *x, const uint32_t *k1, const uint32_t *k2,
+                                           int64_t n, float *out, float *exact, uint8_t *slow)
+{
+    const SgSeg sg{};
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const float2 c = bm_cos_split(a.bm_trig, k2[q]);
+        bool sure;
+        const uint32_t dq = a.bm_rq[k1[q]];
+        (void)opinion_noise_try(a, x[q], bm_radius_estimate(k1[q]), dq, c, &sure);
+        out[q] = opinion_noise(a, sg, a.bm_trig, x[q], dq, k1[q], k2[q]);
+        exact[q] = opinion_noise_pair(a, x[q], a.bm_radius[k1[q]], c);
+        slow[q] = sure ? 0 : 1;
+    }
 }
 
 template <int W>
@@ -625,22 +714,20 @@ __global__ void __launch_bounds__(kOpinionThreads, W == 8 ? 2 : 3) opinion_kerne
             vu[u] = i < tile.end;
             iu[u] = vu[u] ? i : tile.begin; // a valid agent keeps every load in bounds
         }
-        // 1. the normal draw's two Philox integers and the radius
-        uint32_t k1[U], k2[U];
-        float2 r[U];
+        // 1. the normal draw's two Philox integers and the radius correction
+        uint32_t k1[U], k2[U], rq[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const uint32_t lid = seg_lid(sg, iu[u]);
             k1[u] = sg_philox_k23(c0b + 1u, lid, sg.key);
             k2[u] = sg_philox_k23(c0b + 1u + kNormalSalt2, lid, sg.key);
-            r[u] = make_float2(0.0f, 0.0f);
-            if (a.bm_radius) r[u] = a.l2_win ? __ldg(a.bm_radius + k1[u]) : __ldcs(a.bm_radius + k1[u]);
+            rq[u] = a.bm_rq ? __ldg(a.bm_rq + k1[u]) : 0u;
         }
         if (W != 8 || !a.nb8) { // any width, or no neighbour table: one agent at a time
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const float x = opinion_mean<0>(a, sg, xin, iu[u], sg.width);
-                if (vu[u]) xout[iu[u]] = opinion_noise(a, sg, trig, x, r[u], k1[u], k2[u]);
+                if (vu[u]) xout[iu[u]] = opinion_noise(a, sg, trig, x, rq[u], k1[u], k2[u]);
             }
             continue;
         }
@@ -687,7 +774,7 @@ __global__ void __launch_bounds__(kOpinionThreads, W == 8 ? 2 : 3) opinion_kerne
                     norm = __fadd_rn(norm, fabsf(wv[u][j]));
                 }
             const float x = norm > 0.0f ? __fdiv_rn(acc, norm) : xo[u];
-            if (vu[u]) xout[iu[u]] = opinion_noise(a, sg, trig, x, r[u], k1[u], k2[u]);
+            if (vu[u]) xout[iu[u]] = opinion_noise(a, sg, trig, x, rq[u], k1[u], k2[u]);
         }
     }
 }
@@ -781,9 +868,16 @@ static int stride_grid(int64_t work)
     return (int)(b < 1 ? 1 : b > cap ? cap : b);
 }
 
-cudaError_t sg_launch_opinion_tables(float2 *radius, float2 *trig, cudaStream_t st)
+cudaError_t sg_launch_opinion_tables(float2 *radius, uint32_t *rq, float2 *trig, cudaStream_t st)
 {
-    opinion_tables_kernel<<<current_sm_count() * 8, 256, 0, st>>>(radius, trig);
+    opinion_tables_kernel<<<current_sm_count() * 8, 256, 0, st>>>(radius, rq, trig);
+    return cudaGetLastError();
+}
+
+cudaError_t sg_launch_opinion_noise_check(const SgTickArgs &a, const float *x, const uint32_t *k1, const uint32_t *k2,
+                                          int64_t n, float *out, float *exact, uint8_t *slow, cudaStream_t st)
+{
+    opinion_noise_check_kernel<<<stride_grid(n), 256, 0, st>>>(a, x, k1, k2, n, out, exact, slow);
     return cudaGetLastError();
 }
 

@@ -147,7 +147,8 @@ struct SgTickArgs {
     int32_t sweep_wpt;      // class sweep: warps per tile (1, 2 or 4; see sg_sweep_wpt)
     size_t cnt_window;      // count strategy: bytes of cnt to keep in L2 as persisting lines
                             // (an access-policy window on the count kernels); 0 = none
-    const float2 *bm_radius; // opinion: NULL, or the 2^23-entry Box-Muller radius table and
+    const float2 *bm_radius; // opinion: NULL, or the 2^23-entry Box-Muller radius table (pairs),
+    const uint32_t *bm_rq;   // corrections to the step's float32 radius estimates, and
     const float2 *bm_trig;   // the split cosine tables of sg_launch_opinion_tables
     float sigma_hi, sigma_lo; // opinion: the noise sigma as a double-float pair (with the tables)
     const int32_t *nb8;     // opinion, width 8: NULL, or the neighbour table of
@@ -194,15 +195,19 @@ cudaError_t sg_launch_frontier_build(const SgTickArgs &a, bool stats, int grid, 
 cudaError_t sg_launch_frontier_step(const SgTickArgs &a, int variant, bool stats, int grid, cudaStream_t st);
 cudaError_t sg_launch_frontier_scatter(const SgTickArgs &a, int grid, cudaStream_t st);
 cudaError_t sg_launch_opinion(const SgTickArgs &a, int grid, cudaStream_t st, int width);
-// Fills the opinion step's Box-Muller tables, each entry a double-float pair
-// (hi, lo) of float32: radius[k] = sqrt(-2 log(k / 2^23 + 1e-10)) for k < 2^23
-// (64 MiB), and trig = SG_BM_TRIG_ENTRIES pairs: cos of 2 pi j / 2^12 (j < 4096),
-// then cos and sin of 2 pi l / 2^23 (l < 2048), from which the step forms
-// cos(2 pi k / 2^23) by angle addition. radius may be NULL: only the cosine
-// tables are filled.
+// Fills the opinion step's Box-Muller tables: radius[k] = r(k) = sqrt(-2 log(k /
+// 2^23 + 1e-10)) for k < 2^23 as a double-float pair (hi, lo) of float32 (64
+// MiB), rq[k] = (r(k) - e(k)) * 2^40 rounded to an int32 (stored as uint32; 32
+// MiB, SG_BM_RQ_BYTES), where e(k) is the opinion step's own float32 estimate of
+// r(k), and trig =
+// SG_BM_TRIG_ENTRIES pairs: cos of 2 pi j / 2^12 (j < 4096), then cos and sin of
+// 2 pi l / 2^23 (l < 2048), from which the step forms cos(2 pi k / 2^23) by angle
+// addition. radius NULL: only the cosine tables are filled; rq NULL: no
+// fixed-point radii.
 #define SG_BOX_MULLER_SIZE (1 << 23)
 #define SG_BM_TRIG_ENTRIES (4096 + 2 * 2048)
-cudaError_t sg_launch_opinion_tables(float2 *radius, float2 *trig, cudaStream_t st);
+#define SG_BM_RQ_BYTES ((size_t)SG_BOX_MULLER_SIZE * 4)
+cudaError_t sg_launch_opinion_tables(float2 *radius, uint32_t *rq, float2 *trig, cudaStream_t st);
 // nb8[SG_NB8_AT(i, j)] = indices[offsets[i] + j] for j < min(deg(i), 8), else
 // -1: the width-8 opinion step's neighbours, group-major. Agents come in groups
 // of 32 (agent i in group i / 32), each group's table is 256 entries (1 KiB):
@@ -215,6 +220,12 @@ cudaError_t sg_launch_opinion_tables(float2 *radius, float2 *trig, cudaStream_t 
 #define SG_NB8_ENTRIES(n) ((((int64_t)(n) + 31) >> 5) << 8)
 cudaError_t sg_launch_opinion_neighbours8(const int32_t *offsets, const int32_t *indices, int64_t n, int32_t *nb8,
                                           cudaStream_t st);
+// For q < n: out[q] = the opinion step's noise result for opinion x[q] and the
+// draw's integers k1[q], k2[q] < 2^23 (a's Box-Muller tables and sigma set),
+// exact[q] = the result with the pair-table radius, slow[q] = 1 where the
+// fixed-point radius left the float32 rounding open.
+cudaError_t sg_launch_opinion_noise_check(const SgTickArgs &a, const float *x, const uint32_t *k1, const uint32_t *k2,
+                                          int64_t n, float *out, float *exact, uint8_t *slow, cudaStream_t st);
 // out[2 q] = the split-table cosine of k = k0 + q (hi + lo), out[2 q + 1] =
 // cos(2 pi k / 2^23) evaluated directly (q < n).
 cudaError_t sg_launch_opinion_cos_check(const float2 *trig, int32_t k0, int32_t n, double *out, cudaStream_t st);

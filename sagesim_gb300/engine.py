@@ -244,6 +244,22 @@ class Engine:
         self._ck(self._lib.sg_opinion_cosine_check(self._h, int(k0), int(n), _ptr(split), _ptr(direct)))
         return split, direct
 
+    def opinion_noise_check(self, x, k1, k2, sigma):
+        """(result, pair-table result, slow flags) of the opinion step's noise term
+        for opinions x and the normal draw's 23-bit integers k1, k2."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        k1 = np.ascontiguousarray(k1, dtype=np.uint32)
+        k2 = np.ascontiguousarray(k2, dtype=np.uint32)
+        n = len(x)
+        if len(k1) != n or len(k2) != n:
+            raise ValueError("x, k1 and k2 must have the same length")
+        out = np.empty(n, dtype=np.float32)
+        exact = np.empty(n, dtype=np.float32)
+        slow = np.empty(n, dtype=np.uint8)
+        self._ck(self._lib.sg_opinion_noise_check(self._h, float(sigma), n, _ptr(x), _ptr(k1), _ptr(k2),
+                                                  _ptr(out), _ptr(exact), _ptr(slow)))
+        return out, exact, slow.astype(bool)
+
     def profile(self, on=True):
         self._ck(self._lib.sg_profile_enable(self._h, 1 if on else 0))
 

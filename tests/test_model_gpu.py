@@ -326,6 +326,42 @@ def test_opinion_split_cosine_against_direct_cos():
     assert np.abs(direct - host).max() <= 2e-15
 
 
+@pytest.mark.parametrize("sigma", [0.01, 0.25])
+def test_opinion_radius_correction_gives_the_pair_table_result(sigma):
+    """The opinion step forms the Box-Muller radius as a float32 estimate plus a
+    32-bit correction from a table (to 2^-41) and falls back to the double-float
+    pair table only where that leaves the float32 rounding of x + sigma * r *
+    cos open. Over every one of the 2^23 radii (opinions spread over [0, 1],
+    near 0 and 1, tiny, negative, and tiny radii with tiny opinions, where
+    float32 steps are finest) the result equals the pair-table result bit for
+    bit, the fallback is rare but taken, and the result matches the reference's
+    double expression (sagesim/math_utils.py:231-255) rounded to float32 within
+    one ulp, almost always exactly."""
+    rng = np.random.default_rng(11)
+    n = 1 << 23
+    q = n // 6
+    x = np.concatenate([rng.random(q), rng.uniform(-0.1, 0.1, q), rng.uniform(0.9, 1.1, q),
+                        10.0 ** -rng.uniform(1, 8, q), 10.0 ** -rng.uniform(5, 12, q),
+                        rng.uniform(0.45, 0.55, n - 5 * q)]).astype(np.float32)
+    k1 = rng.permutation(n).astype(np.uint32)  # every radius once
+    k2 = rng.integers(0, 1 << 23, n, dtype=np.uint32)
+    tiny = np.flatnonzero(k1 >= (1 << 23) - 4096)  # radii below 0.03 ...
+    x[tiny] = (10.0 ** -rng.uniform(5, 12, tiny.size)).astype(np.float32)  # ... with tiny opinions
+    with Engine() as e:
+        out, exact, slow = e.opinion_noise_check(x, k1, k2, sigma)
+    assert np.array_equal(out.view(np.uint32), exact.view(np.uint32))
+    assert slow.any()  # about 60 of the 2^23 at sigma 0.01
+    assert slow[:q].mean() < 1e-4, slow[:q].mean()
+    assert slow.mean() < 1e-3, slow.mean()
+    r = np.sqrt(-2.0 * np.log(k1 / 8388608.0 + 1e-10))
+    c = np.cos(6.283185307179586 * (k2 / 8388608.0))
+    want = np.clip((x.astype(np.float64) + sigma * (r * c)).astype(np.float32), 0.0, 1.0).astype(np.float32)
+    want[want == 0] = 0.0
+    ulp = np.abs(out.view(np.int32).astype(np.int64) - want.view(np.int32).astype(np.int64))
+    assert ulp.max() <= 1
+    assert (ulp != 0).mean() < 1e-5
+
+
 def test_opinion_long_run_stays_within_tolerance():
     """500 ticks (the benchmark's run length) on a 50,000-agent WS graph: the
     opinions stay within 1e-6 relative of the oracle at ticks 100, 250 and 500."""
