@@ -150,13 +150,14 @@ typedef struct sg_tune {
                                /*      0-2 in busy ticks (decided on the GPU;    */
                                /*      graphs of 24+ tiles per SM, or with 32)   */
                                /* 512 = flat draws in place of the loop form     */
-                               /*      (in-place runs): a block lays its tile's  */
-                               /*      draws end to end, each thread an equal    */
+                               /*      (in-place runs): a warp lays its agents'  */
+                               /*      draws end to end, each lane an equal      */
                                /*      share                                     */
                                /* default 790: class sweep + hybrid whose busy-  */
-                               /*      tick form is the flat draws (the loop     */
-                               /*      form's bits 2 and 4 apply where flat      */
-                               /*      draws cannot run: runs not in place)      */
+                               /*      tick form is the flat draws, both in one  */
+                               /*      launch per tick (the loop form's bits 2   */
+                               /*      and 4 apply where flat draws cannot run:  */
+                               /*      runs not in place)                        */
     double us_per_tick;        /* measured by sg_batch_tune (output)             */
 } sg_tune;
 

@@ -516,8 +516,19 @@ struct SgSweepTile {
     unsigned long long *stats;
 };
 
+// Shared memory of the class sweep with WPT warps per tile.
+template <int WPT>
+struct SgSweepSmem {
+    uint16_t cand[kWarps][SG_TILE]; // slot | infected << 11
+    SgSweepTile tp[kWarps];
+    int32_t ccount[kWarps], nch[kWarps / WPT];
+    unsigned long long dstat[kWarps][3]; // per warp region: S, I, R changes (mod 2^64)
+};
+
+// One tick of the class sweep over the launch's tiles (the caller has decided
+// that this form takes the tick).
 template <int VARIANT, bool STATS, int WPT>
-__global__ void __launch_bounds__(SG_SIR_THREADS, 5) sir_count_sweep_kernel(SgTickArgs a)
+__device__ __forceinline__ void sweep_tick(const SgTickArgs &a, SgSweepSmem<WPT> &sm)
 {
     constexpr int kRun = 16;                     // agents per lane and class load
     constexpr int kRuns = SG_TILE / (32 * kRun); // runs of a whole tile per lane
@@ -527,11 +538,11 @@ __global__ void __launch_bounds__(SG_SIR_THREADS, 5) sir_count_sweep_kernel(SgTi
     static_assert(kRuns * 32 * kRun == SG_TILE, "runs must cover the tile");
     static_assert(kMyRuns * WPT == kRuns && TPB * WPT == kWarps, "warps must split tiles evenly");
     static_assert(SG_TILE <= 0x800, "slot must fit in 11 bits");
-    __shared__ uint16_t sh_cand[kWarps][SG_TILE]; // slot | infected << 11
-    __shared__ SgSweepTile sh_tp[kWarps];
-    __shared__ int32_t sh_ccount[kWarps], sh_nch[TPB];
-    __shared__ unsigned long long sh_dstat[kWarps][3]; // per warp region: S, I, R changes (mod 2^64)
-    if (hybrid_loop_tick(a)) return; // the loop form takes this tick
+    auto &sh_cand = sm.cand;
+    auto &sh_tp = sm.tp;
+    auto &sh_ccount = sm.ccount;
+    auto &sh_nch = sm.nch;
+    auto &sh_dstat = sm.dstat;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int ti = warp / WPT, part = warp % WPT; // this warp's tile in the group and part of it
     int32_t *const state = (int32_t *)a.buf0;
@@ -785,6 +796,32 @@ __global__ void __launch_bounds__(SG_SIR_THREADS, 5) sir_count_sweep_kernel(SgTi
     }
 }
 
+template <int VARIANT, bool STATS, int WPT>
+__global__ void __launch_bounds__(SG_SIR_THREADS, 5) sir_count_sweep_kernel(SgTickArgs a)
+{
+    __shared__ SgSweepSmem<WPT> sm;
+    if (hybrid_loop_tick(a)) return; // the loop form takes this tick
+    sweep_tick<VARIANT, STATS, WPT>(a, sm);
+}
+
+// The hybrid step with flat draws in one launch: the class sweep in quiet
+// ticks and flat draws in busy ones (hybrid_loop_tick gives every block the
+// same answer), so no idle kernel is launched per tick. Shared memory is the
+// larger of the two forms' (they never run in the same launch).
+template <int WPT>
+union SgHybridSmem {
+    SgSweepSmem<WPT> sweep;
+    SgFlatSmem flat;
+};
+
+template <int VARIANT, bool STATS, int WPT>
+__global__ void __launch_bounds__(SG_SIR_THREADS, kFlatBlocksPerSm) sir_count_hybrid_kernel(SgTickArgs a)
+{
+    __shared__ SgHybridSmem<WPT> sm;
+    if (hybrid_loop_tick(a)) flat_tick<VARIANT, STATS>(a, sm.flat);
+    else sweep_tick<VARIANT, STATS, WPT>(a, sm.sweep);
+}
+
 // ---- scatter -------------------------------------------------------------------------
 // +-1 along the transpose rows of up to 32 changes, one per lane (b, e: the
 // lane's row; empty for no change).
@@ -1031,6 +1068,26 @@ cudaError_t sg_launch_sir_count_step(const SgTickArgs &args, int variant, bool s
     if (nlaunched) *nlaunched = 1;
     const bool sweep = (a.flavour & SG_FLAVOUR_SWEEP) && inplace && a.cls && a.chunks;
     if (!sweep) a.hybrid_rise = 0; // the loop form takes every tick
+    if (sweep && a.hybrid_rise > 0 && (a.flavour & SG_FLAVOUR_FLAT)) {
+        // sweep and flat draws in one launch; the grid is the flat form's (two
+        // blocks per resident slot), the sweep's groups are spread over it
+        const int wpt = a.sweep_wpt == 2 || a.sweep_wpt == 4 ? a.sweep_wpt : 1;
+        int dev = 0, sms = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+            return cudaErrorInvalidDevice;
+        const int hgrid = std::max(1, std::min(grid, 2 * kFlatBlocksPerSm * sms));
+#define SG_HY(V, S, W) launch_count_kernel(sir_count_hybrid_kernel<V, S, W>, a, hgrid, st)
+#define SG_HYW(V, S) (wpt == 1 ? SG_HY(V, S, 1) : wpt == 2 ? SG_HY(V, S, 2) : SG_HY(V, S, 4))
+        if (variant == 1) {
+            if (stats) SG_HYW(1, true); else SG_HYW(1, false);
+        } else {
+            if (stats) SG_HYW(2, true); else SG_HYW(2, false);
+        }
+#undef SG_HYW
+#undef SG_HY
+        return cudaGetLastError();
+    }
     if (sweep) {
         const int wpt = a.sweep_wpt == 2 || a.sweep_wpt == 4 ? a.sweep_wpt : 1;
         const int tpb = kWarps / wpt;

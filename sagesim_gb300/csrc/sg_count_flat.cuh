@@ -51,24 +51,36 @@ __device__ __forceinline__ void philox_k23_ilp(uint32_t (&c0)[U], uint32_t (&c1)
     for (int u = 0; u < U; ++u) c0[u] &= 0x7FFFFFu;
 }
 
+// Shared memory of the flat step, per warp: its candidates' first draws
+// ([ncand] = the warp's draws), RNG keys, Philox counter bases (counter of draw
+// d = base + d), agent (0..255) | 0x100 for a recovery, and a hit bit per agent.
+struct SgFlatSmem {
+    int32_t start[kWarps][kFlatWarpAgents + 1];
+    uint32_t lid[kWarps][kFlatWarpAgents];
+    uint32_t base[kWarps][kFlatWarpAgents];
+    uint16_t info[kWarps][kFlatWarpAgents];
+    uint32_t hit[kWarps][kFlatWarpAgents / 32];
+    int32_t nw[kWarps], coff[kWarps], cbase;
+    unsigned long long red[4][kWarps];
+};
+
+// One tick of flat draws over the launch's tiles (the caller has decided that
+// this form takes the tick).
 template <int VARIANT, bool STATS>
-__global__ void __launch_bounds__(SG_SIR_THREADS, kFlatBlocksPerSm) sir_count_flat_kernel(SgTickArgs a)
+__device__ __forceinline__ void flat_tick(const SgTickArgs &a, SgFlatSmem &sm)
 {
-    if (a.hybrid_rise > 0) {
-        if (!hybrid_loop_tick(a)) return; // the class sweep takes this tick
-        // activity bits owed a rebuild stay owed until a sweep tick rebuilds them
-        if (blockIdx.x == 0 && threadIdx.x == 0 && a.mrebuild && a.mrebuild[a.r]) a.mrebuild[a.r + 1] = 1;
-    }
-    // per warp: its candidates' first draws ([ncand] = the warp's draws), RNG
-    // keys, Philox counter bases (counter of draw d = base + d), agent (0..255)
-    // | 0x100 for a recovery, and a hit bit per agent
-    __shared__ int32_t sh_start[kWarps][kFlatWarpAgents + 1];
-    __shared__ uint32_t sh_lid[kWarps][kFlatWarpAgents];
-    __shared__ uint32_t sh_base[kWarps][kFlatWarpAgents];
-    __shared__ uint16_t sh_info[kWarps][kFlatWarpAgents];
-    __shared__ uint32_t sh_hit[kWarps][kFlatWarpAgents / 32];
-    __shared__ int32_t sh_nw[kWarps], sh_coff[kWarps], sh_cbase;
-    __shared__ unsigned long long red[4][kWarps];
+    // activity bits owed a rebuild stay owed until a sweep tick rebuilds them
+    if (a.hybrid_rise > 0 && blockIdx.x == 0 && threadIdx.x == 0 && a.mrebuild && a.mrebuild[a.r])
+        a.mrebuild[a.r + 1] = 1;
+    auto &sh_start = sm.start;
+    auto &sh_lid = sm.lid;
+    auto &sh_base = sm.base;
+    auto &sh_info = sm.info;
+    auto &sh_hit = sm.hit;
+    auto &sh_nw = sm.nw;
+    auto &sh_coff = sm.coff;
+    auto &sh_cbase = sm.cbase;
+    auto &red = sm.red;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     int32_t cur_seg = -1;
     int64_t tick = 0, end_tick = 0;
@@ -344,4 +356,12 @@ __global__ void __launch_bounds__(SG_SIR_THREADS, kFlatBlocksPerSm) sir_count_fl
                 a.chunks[base + j] = SgChunk{wfirst + 32 * j, min(32, nw - 32 * j)};
         }
     }
+}
+
+template <int VARIANT, bool STATS>
+__global__ void __launch_bounds__(SG_SIR_THREADS, kFlatBlocksPerSm) sir_count_flat_kernel(SgTickArgs a)
+{
+    __shared__ SgFlatSmem sm;
+    if (a.hybrid_rise > 0 && !hybrid_loop_tick(a)) return; // the class sweep takes this tick
+    flat_tick<VARIANT, STATS>(a, sm);
 }

@@ -53,8 +53,9 @@ struct SgMega {
                               // busy ticks (see SgTickArgs::hybrid_rise/fall and
                               // sg_hybrid_thresholds)
 #define SG_FLAVOUR_FLAT 512   // flat draws in place of the loop form (in-place runs): a
-                              // block lays its tile's draws end to end and each thread
-                              // takes an equal share
+                              // warp lays its agents' draws end to end and each lane
+                              // takes an equal share; with SWEEP and HYBRID, both forms
+                              // run in one launch
 #define SG_FLAVOUR_MAX 1023
 // The class sweep runs one warp per tile; below this many tiles per SM it
 // leaves SMs idle and the loop form (lazy loads) is used instead, unless
@@ -66,7 +67,7 @@ struct SgMega {
 // share a tile so that smaller graphs still fill the SMs.
 // Change-count thresholds of the hybrid count step for a launch over ntiles
 // tiles (the crossovers measured on a 10^7-agent power-law epidemic: about one
-// change per 400 agents while it grows, one per 36 while it declines). The
+// change per 400 agents while it grows, one per 60 while it declines). The
 // unchosen kernel's launch costs about 2.5 us per tick, which smaller graphs
 // do not earn back (measured at 10^6 and 2.5 10^6 agents), so the hybrid runs
 // from SG_HYBRID_MIN_TILES_PER_SM tiles per SM.
@@ -77,7 +78,7 @@ inline void sg_hybrid_thresholds(int64_t ntiles, int sm_count, int32_t flavour, 
     const bool on = (flavour & SG_FLAVOUR_HYBRID) && (flavour & SG_FLAVOUR_SWEEP) &&
                     ((flavour & SG_FLAVOUR_FORCE) || ntiles >= (int64_t)sm_count * SG_HYBRID_MIN_TILES_PER_SM);
     *rise = on ? (int32_t)(n / 400 > 0 ? n / 400 : 1) : 0;
-    *fall = on ? (int32_t)(n / 36 > 0 ? n / 36 : 1) : 0;
+    *fall = on ? (int32_t)(n / 60 > 0 ? n / 60 : 1) : 0;
 }
 
 inline int32_t sg_sweep_wpt(int64_t ntiles, int sm_count, int32_t flavour)
