@@ -947,39 +947,48 @@ __device__ __forceinline__ void scatter_changes(const SgTickArgs &a, int32_t fir
         scatter_rows_lane(a, b, e, delta, lane, sb);
 }
 
-// The tick's long-row segments (kSegRow entries each), one per warp.
-__device__ __forceinline__ void scatter_row_segments(const SgTickArgs &a, int lane, int warp_id, int nwarps, bool sb)
+// One long-row segment (kSegRow entries) by one warp.
+__device__ __forceinline__ void scatter_row_segment(const SgTickArgs &a, const SgRowSeg &sgm, int lane, bool sb)
 {
-    const int32_t nsg = a.nrowsegs[a.r];
-    for (int32_t w = warp_id; w < nsg; w += nwarps) {
-        const SgRowSeg sgm = a.rowsegs[w];
-        for (int32_t k0 = sgm.begin; k0 < sgm.end; k0 += 32 * kScatterUnroll) {
-            int32_t d[kScatterUnroll];
+    for (int32_t k0 = sgm.begin; k0 < sgm.end; k0 += 32 * kScatterUnroll) {
+        int32_t d[kScatterUnroll];
 #pragma unroll
-            for (int u = 0; u < kScatterUnroll; ++u) {
-                const int32_t k = k0 + u * 32 + lane;
-                d[u] = k < sgm.end ? __ldg(a.tidx + k) : -1;
-            }
-#pragma unroll
-            for (int u = 0; u < kScatterUnroll; ++u)
-                if (d[u] >= 0) count_add(a, d[u], sgm.delta, sb);
+        for (int u = 0; u < kScatterUnroll; ++u) {
+            const int32_t k = k0 + u * 32 + lane;
+            d[u] = k < sgm.end ? __ldg(a.tidx + k) : -1;
         }
+#pragma unroll
+        for (int u = 0; u < kScatterUnroll; ++u)
+            if (d[u] >= 0) count_add(a, d[u], sgm.delta, sb);
     }
 }
 
+// The tick's long-row segments, one per warp.
+__device__ __forceinline__ void scatter_row_segments(const SgTickArgs &a, int lane, int warp_id, int nwarps, bool sb)
+{
+    const int32_t nsg = a.nrowsegs[a.r];
+    for (int32_t w = warp_id; w < nsg; w += nwarps) scatter_row_segment(a, a.rowsegs[w], lane, sb);
+}
+
 // Work-list form: warps take the tick's non-empty 32-change chunks, so a tile
-// with thousands of changes is spread over many warps.
+// with thousands of changes is spread over many warps, and then the long-row
+// segments, as one list (segments continue where the chunks end, so the warps
+// that took chunks are not also the ones that take the segments).
 template <bool LB>
 __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_scatter_chunks_kernel(SgTickArgs a)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int32_t nck = a.nchunks[a.r];
+    const int32_t nitems = nck + (a.rowsegs ? a.nrowsegs[a.r] : 0);
     const bool sb = scatter_sets_bits(a);
-    for (int32_t w = blockIdx.x * kWarps + warp; w < nck; w += gridDim.x * kWarps) {
-        const SgChunk ck = a.chunks[w];
-        scatter_changes<LB>(a, ck.first, 0, ck.count, lane, sb);
+    for (int32_t w = blockIdx.x * kWarps + warp; w < nitems; w += gridDim.x * kWarps) {
+        if (w < nck) {
+            const SgChunk ck = a.chunks[w];
+            scatter_changes<LB>(a, ck.first, 0, ck.count, lane, sb);
+        } else {
+            scatter_row_segment(a, a.rowsegs[w - nck], lane, sb);
+        }
     }
-    if (a.rowsegs) scatter_row_segments(a, lane, blockIdx.x * kWarps + warp, gridDim.x * kWarps, sb);
 }
 
 // Per-tile form (no work list): blocks walk the tiles and their warps the
