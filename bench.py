@@ -44,11 +44,11 @@ SEED = 1
 # dram__bytes_write.sum, averaged over all 200 ticks of one simulate, L2 contents kept
 # from launch to launch as in the run), from
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum \
-#       --cache-control none --clock-control none --csv --log-file dram.csv \
-#       python bench.py --profile-case
-# keyed by (strategy, agents, kernel); the count step is the sum of both hybrid kernels
-# per tick. Re-measure when a kernel changes.
-MEASURED_TRAFFIC = {("count", 10_000_000, "sir_count_step"): 37.219e6}
+#       --cache-control none --clock-control none -k regex:sir_count_hybrid -c 200 \
+#       --csv --log-file dram.csv python bench.py --profile-case
+# keyed by (strategy, agents, kernel); the count step is one launch per tick (class
+# sweep or flat draws). Re-measure when a kernel changes.
+MEASURED_TRAFFIC = {("count", 10_000_000, "sir_count_step"): 29.996e6}
 PARTS = 64
 CODES = (1, 2, 3)
 WORKLOAD = ("SIR per-infected-neighbour (salt 2+j trials), BA n=%d m=4 seed 1, 64-way locality relabel, "
