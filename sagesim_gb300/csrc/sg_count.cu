@@ -477,6 +477,14 @@ __global__ void __launch_bounds__(SG_SIR_THREADS) sir_count_step_kernel(SgTickAr
     }
 }
 
+// Bits 0-3: which of the four class bytes of w equal c (a byte equal to c
+// becomes 0xFF under the SIMD compare; the bytes' low bits are gathered by one
+// multiply).
+__device__ __forceinline__ uint32_t class_mask4(uint32_t w, uint32_t c)
+{
+    return ((__vcmpeq4(w, c * 0x01010101u) & 0x01010101u) * 0x01020408u) >> 24;
+}
+
 // ---- count step, flat draws (busy ticks) -----------------------------------------------
 #include "sg_count_flat.cuh"
 
@@ -600,13 +608,13 @@ __device__ __forceinline__ void sweep_tick(const SgTickArgs &a, SgSweepSmem<WPT>
                             }
                     }
                     const uint32_t bits = nv > 0 ? (a.amask[b >> 5] >> (b & 31)) & 0xFFFFu : 0u;
+                    // class bytes compared four at a time: bit e of each mask is agent e
                     uint32_t sm = 0, imr = 0, rm = 0;
 #pragma unroll
-                    for (int e = 0; e < kRun; ++e) {
-                        const uint32_t c = (w[e >> 2] >> (8 * (e & 3))) & 0xFFu;
-                        sm |= (uint32_t)(c == 0u) << e;
-                        imr |= (uint32_t)(c == 1u) << e;
-                        rm |= (uint32_t)(c == 2u) << e;
+                    for (int q = 0; q < 4; ++q) {
+                        sm |= class_mask4(w[q], 0u) << (4 * q);
+                        imr |= class_mask4(w[q], 1u) << (4 * q);
+                        if (STATS) rm |= class_mask4(w[q], 2u) << (4 * q);
                     }
                     if (rebuild) {
                         // lanes 2j and 2j + 1 hold the 32 agents of one mask word

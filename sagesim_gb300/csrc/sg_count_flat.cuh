@@ -172,10 +172,8 @@ __device__ __forceinline__ void flat_tick(const SgTickArgs &a, SgFlatSmem &sm)
         //    class bytes compared four at a time: a byte equal to 0 or 1 becomes
         //    0xFF, and the bytes' low bits are gathered into a mask)
         const uint32_t cl_lo = (uint32_t)cw, cl_hi = (uint32_t)(cw >> 32);
-        auto byte_mask = [](uint32_t v) -> uint32_t { return ((v & 0x01010101u) * 0x01020408u) >> 24; };
-        const uint32_t smask = byte_mask(__vcmpeq4(cl_lo, 0u)) | (byte_mask(__vcmpeq4(cl_hi, 0u)) << 4);
-        const uint32_t imask =
-            byte_mask(__vcmpeq4(cl_lo, 0x01010101u)) | (byte_mask(__vcmpeq4(cl_hi, 0x01010101u)) << 4);
+        const uint32_t smask = class_mask4(cl_lo, 0u) | (class_mask4(cl_hi, 0u) << 4);
+        const uint32_t imask = class_mask4(cl_lo, 1u) | (class_mask4(cl_hi, 1u) << 4);
         uint32_t cand = imask, more = 0;
         int32_t ndraw = __popc(imask);
 #pragma unroll
