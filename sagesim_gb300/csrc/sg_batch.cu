@@ -200,7 +200,7 @@ int SgPool::allocate(int64_t acap, int64_t ecap, int64_t max_scen, bool transpos
     POOL_CK(changes.reserve((size_t)std::max<int64_t>(acap, 1) * 4));
     POOL_CK(tile_nch.reserve((size_t)tile_cap * 4));
     POOL_CK(chunks.reserve(((size_t)acap / 32 + (size_t)tile_cap + 1) * sizeof(SgChunk)));
-    POOL_CK(rowsegs.reserve(((size_t)ecap / 128 + 64) * sizeof(SgRowSeg)));
+    POOL_CK(rowsegs.reserve(SG_ROWSEG_CAPACITY(ecap) * sizeof(SgRowSeg)));
     POOL_CK(tiles.reserve((size_t)tile_cap * sizeof(SgTile)));
     POOL_CK(segs.reserve((size_t)seg_cap * sizeof(SgSeg)));
     any_lids = with_lids;

@@ -236,7 +236,7 @@ __device__ __forceinline__ bool hybrid_loop_tick(const SgTickArgs &a)
 // A changed agent whose transpose row is longer than kSegRow is handed to the
 // scatter as row segments of kSegRow entries on their own work list, so no
 // single warp walks a hub's whole row; the chunk pass skips such rows.
-constexpr int32_t kSegRow = 256;
+constexpr int32_t kSegRow = SG_SEG_ROW;
 
 // What the scatter needs of changed agent g, whose change-list entry is
 // `slot`: a long transpose row goes to the segment list (its recorded row is

@@ -913,7 +913,7 @@ static int prepare_run(sg_engine *e, const SgPlan &pl, int64_t tick0, int32_t nt
         SG_CK(e->tile_nch.reserve((size_t)std::max(pl.count_step->ntiles, 1) * 4));
         SG_CK(e->chunks.reserve(((size_t)e->n / 32 + pl.count_step->ntiles + 1) * sizeof(SgChunk)));
         SG_CK(e->nchunks.reserve((size_t)std::max(nticks, 1) * 4));
-        SG_CK(e->rowsegs.reserve(((size_t)e->nnz / 128 + 64) * sizeof(SgRowSeg)));
+        SG_CK(e->rowsegs.reserve(SG_ROWSEG_CAPACITY(e->nnz) * sizeof(SgRowSeg)));
         SG_CK(e->nrowsegs.reserve((size_t)std::max(nticks, 1) * 4));
     }
     // class bytes and activity bits: kept by every count-strategy kernel, read by

@@ -91,6 +91,14 @@ inline int32_t sg_sweep_wpt(int64_t ntiles, int sm_count, int32_t flavour)
     return 4;
 }
 
+// The count scatter hands a changed agent's transpose row longer than
+// SG_SEG_ROW entries to its segment list as pieces of SG_SEG_ROW entries, so no
+// warp walks a long row alone. A tick changes each agent at most once, and a
+// row of L > SG_SEG_ROW entries gives at most 2 L / SG_SEG_ROW pieces, so a
+// tick's list holds at most SG_ROWSEG_CAPACITY(nnz) segments.
+#define SG_SEG_ROW 64
+#define SG_ROWSEG_CAPACITY(nnz) (2 * (size_t)(nnz) / SG_SEG_ROW + 64)
+
 // One warp's share of the scatter: change-list entries [first, first + count),
 // count <= 32 (a tile's changes in runs of 32).
 struct SgChunk {
