@@ -280,8 +280,11 @@ __device__ __forceinline__ void flat_tick(const SgTickArgs &a, SgFlatSmem &sm)
                 }
             }
         }
-        // 6. transitions: state in place, class byte; then this warp's part of the
-        //    change list (entry and row)
+        // 6. transitions: the warp's changed agents are listed in shared memory
+        //    (the candidate records are no longer read), then each lane applies
+        //    every 32nd: state in place, class byte, change-list entry and row.
+        //    Changes are sparse, so this runs one or two rounds instead of a
+        //    pass over each lane's 8 agents.
         int32_t nw = 0;
         if (__any_sync(FULL_MASK, hits)) {
             const int32_t nh = __popc(hits);
@@ -292,18 +295,21 @@ __device__ __forceinline__ void flat_tick(const SgTickArgs &a, SgFlatSmem &sm)
                 if (lane >= o) incl += y;
             }
             nw = __shfl_sync(FULL_MASK, incl, 31);
-            int32_t pos = wfirst + incl - nh;
+            uint16_t *const hl = sh_info[warp]; // agent in the warp's 256 | 0x100 for a recovery
+            int32_t pos = incl - nh;
 #pragma unroll
             for (int e = 0; e < kFlatPer; ++e)
-                if ((hits >> e) & 1u) {
-                    const int32_t i = b0 + e;
-                    const bool rec = (imask >> e) & 1u;
-                    state[i] = rec ? cr : ci;
-                    if (a.cls) a.cls[i] = (uint8_t)(rec ? 2 : 1);
-                    a.changes[pos] = rec ? ~i : i;
-                    record_changed_row(a, pos, i, rec ? -1 : 1);
-                    ++pos;
-                }
+                if ((hits >> e) & 1u) hl[pos++] = (uint16_t)((lane * kFlatPer + e) | (((imask >> e) & 1u) << 8));
+            __syncwarp();
+            for (int32_t q = lane; q < nw; q += 32) {
+                const uint32_t h = hl[q];
+                const int32_t i = wfirst + (int32_t)(h & 0xFFu);
+                const bool rec = (h >> 8) != 0;
+                state[i] = rec ? cr : ci;
+                if (a.cls) a.cls[i] = (uint8_t)(rec ? 2 : 1);
+                a.changes[wfirst + q] = rec ? ~i : i;
+                record_changed_row(a, wfirst + q, i, rec ? -1 : 1);
+            }
         }
         if (STATS) {
             unsigned long long nS = 0, nI = 0, nR = 0, eS = 0;
