@@ -9,7 +9,7 @@
 // the draws of its 256 agents' candidates end to end (a warp scan of the
 // per-lane draw counts) and every lane evaluates an equal, contiguous share of
 // that sequence: it finds the owner of its first draw by a binary search over
-// the candidates' starts in the warp's part of shared memory and walks forward,
+// the candidates' draw ends in the warp's part of shared memory and walks forward,
 // four Philox chains in flight. The draws of one candidate may be split
 // between lanes; all are evaluated (the outcome depends only on whether some
 // draw j < k is below beta, so no order or early exit is needed). Hits are
@@ -51,14 +51,12 @@ __device__ __forceinline__ void philox_k23_ilp(uint32_t (&c0)[U], uint32_t (&c1)
     for (int u = 0; u < U; ++u) c0[u] &= 0x7FFFFFu;
 }
 
-// Shared memory of the flat step, per warp: its candidates' first draws
-// ([ncand] = the warp's draws), RNG keys, Philox counter bases (counter of draw
-// d = base + d), agent (0..255) | 0x100 for a recovery, and a hit bit per agent.
+// Shared memory of the flat step, per warp: one 16-byte record per candidate
+// (Philox counter base: the counter of draw d is base + d; RNG key; threshold;
+// end of its draws in the warp's sequence | agent 0..255 << 16, so advancing to
+// the next candidate is one load) and a hit bit per agent.
 struct SgFlatSmem {
-    int32_t start[kWarps][kFlatWarpAgents + 1];
-    uint32_t lid[kWarps][kFlatWarpAgents];
-    uint32_t base[kWarps][kFlatWarpAgents];
-    uint16_t info[kWarps][kFlatWarpAgents];
+    uint4 rec[kWarps][kFlatWarpAgents];
     uint32_t hit[kWarps][kFlatWarpAgents / 32];
     int32_t nw[kWarps], coff[kWarps], cbase;
     unsigned long long red[4][kWarps];
@@ -72,10 +70,7 @@ __device__ __forceinline__ void flat_tick(const SgTickArgs &a, SgFlatSmem &sm)
     // activity bits owed a rebuild stay owed until a sweep tick rebuilds them
     if (a.hybrid_rise > 0 && blockIdx.x == 0 && threadIdx.x == 0 && a.mrebuild && a.mrebuild[a.r])
         a.mrebuild[a.r + 1] = 1;
-    auto &sh_start = sm.start;
-    auto &sh_lid = sm.lid;
-    auto &sh_base = sm.base;
-    auto &sh_info = sm.info;
+    auto &sh_rec = sm.rec;
     auto &sh_hit = sm.hit;
     auto &sh_nw = sm.nw;
     auto &sh_coff = sm.coff;
@@ -201,17 +196,16 @@ __device__ __forceinline__ void flat_tick(const SgTickArgs &a, SgFlatSmem &sm)
             for (int e = 0; e < kFlatPer; ++e)
                 if ((cand >> e) & 1u) {
                     const bool rec = (imask >> e) & 1u;
-                    sh_start[warp][cpos] = dpos;
-                    sh_info[warp][cpos] = (uint16_t)((lane * kFlatPer + e) | (rec ? 0x100 : 0));
-                    sh_lid[warp][cpos] = l[e];
+                    const int32_t dn = dpos + (rec || VARIANT == 1 ? 1 : min(k[e], kFlatCap));
                     // Philox counter of draw d is base + d: salt 1 for a recovery
                     // (and SIR-A), salt 2 + j for the j-th SIR-B draw
-                    sh_base[warp][cpos] = c0b + (rec || VARIANT == 1 ? 1u : 2u) - (uint32_t)dpos;
+                    sh_rec[warp][cpos] = make_uint4(c0b + (rec || VARIANT == 1 ? 1u : 2u) - (uint32_t)dpos, l[e],
+                                                    rec ? krec : kinf,
+                                                    (uint32_t)dn | ((uint32_t)(lane * kFlatPer + e) << 16));
                     ++cpos;
-                    dpos += rec || VARIANT == 1 ? 1 : min(k[e], kFlatCap);
+                    dpos = dn;
                 }
         }
-        if (lane == 0) sh_start[warp][ncand] = ntot;
         if (lane < kFlatWarpAgents / 32) sh_hit[warp][lane] = 0u;
         __syncwarp();
         // 4. an equal share of the warp's draws per lane, kFlatIlp side by side
@@ -220,46 +214,39 @@ __device__ __forceinline__ void flat_tick(const SgTickArgs &a, SgFlatSmem &sm)
             int32_t d = lane * per;
             const int32_t dend = min(d + per, ntot);
             if (d < dend) {
-                const int32_t *starts = sh_start[warp];
-                int32_t lo = 0, hi = ncand - 1; // owner of draw d: the last c with starts[c] <= d
+                const uint4 *recs = sh_rec[warp];
+                int32_t lo = 0, hi = ncand - 1; // owner of draw d: the first c whose draws end after d
                 while (lo < hi) {
-                    const int32_t mid = (lo + hi + 1) >> 1;
-                    if (starts[mid] <= d) lo = mid;
-                    else hi = mid - 1;
+                    const int32_t mid = (lo + hi) >> 1;
+                    if ((int32_t)(recs[mid].w & 0xFFFFu) > d) hi = mid;
+                    else lo = mid + 1;
                 }
                 int32_t c = lo;
-                int32_t cend = starts[c + 1];
-                uint32_t info = sh_info[warp][c], clid = sh_lid[warp][c], cbase = sh_base[warp][c];
+                uint4 cr4 = recs[c]; // counter base, RNG key, threshold, end of draws | agent << 16
                 // every candidate has at least one draw, so consecutive draws
                 // belong to the same candidate or to the next one
                 auto next = [&](int32_t dd) {
-                    if (dd >= cend) {
-                        ++c;
-                        cend = starts[c + 1];
-                        info = sh_info[warp][c];
-                        clid = sh_lid[warp][c];
-                        cbase = sh_base[warp][c];
-                    }
+                    if (dd >= (int32_t)(cr4.w & 0xFFFFu)) cr4 = recs[++c];
                 };
                 for (; d + kFlatIlp <= dend; d += kFlatIlp) {
                     uint32_t c0[kFlatIlp], c1[kFlatIlp], th[kFlatIlp], in[kFlatIlp];
 #pragma unroll
                     for (int u = 0; u < kFlatIlp; ++u) {
                         next(d + u);
-                        c0[u] = cbase + (uint32_t)(d + u);
-                        c1[u] = clid;
-                        th[u] = (info & 0x100u) ? krec : kinf;
-                        in[u] = info;
+                        c0[u] = cr4.x + (uint32_t)(d + u);
+                        c1[u] = cr4.y;
+                        th[u] = cr4.z;
+                        in[u] = cr4.w >> 16;
                     }
                     philox_k23_ilp<kFlatIlp>(c0, c1, ks);
 #pragma unroll
                     for (int u = 0; u < kFlatIlp; ++u)
-                        if (c0[u] < th[u]) atomicOr(&sh_hit[warp][(in[u] & 0xFFu) >> 5], 1u << (in[u] & 31u));
+                        if (c0[u] < th[u]) atomicOr(&sh_hit[warp][in[u] >> 5], 1u << (in[u] & 31u));
                 }
                 for (; d < dend; ++d) { // the last few, one at a time
                     next(d);
-                    if (sg_philox_k23_keys(cbase + (uint32_t)d, clid, ks) < ((info & 0x100u) ? krec : kinf))
-                        atomicOr(&sh_hit[warp][(info & 0xFFu) >> 5], 1u << (info & 31u));
+                    if (sg_philox_k23_keys(cr4.x + (uint32_t)d, cr4.y, ks) < cr4.z)
+                        atomicOr(&sh_hit[warp][(cr4.w >> 16) >> 5], 1u << ((cr4.w >> 16) & 31u));
                 }
             }
         }
@@ -295,7 +282,8 @@ __device__ __forceinline__ void flat_tick(const SgTickArgs &a, SgFlatSmem &sm)
                 if (lane >= o) incl += y;
             }
             nw = __shfl_sync(FULL_MASK, incl, 31);
-            uint16_t *const hl = sh_info[warp]; // agent in the warp's 256 | 0x100 for a recovery
+            // agent in the warp's 256 | 0x100 for a recovery (over the candidate records)
+            uint16_t *const hl = reinterpret_cast<uint16_t *>(sh_rec[warp]);
             int32_t pos = incl - nh;
 #pragma unroll
             for (int e = 0; e < kFlatPer; ++e)
