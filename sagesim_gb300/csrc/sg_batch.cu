@@ -92,7 +92,8 @@ int64_t sg_pool_scenario_bytes(int64_t n, int64_t nnz, bool transpose, bool lids
                               (lids ? 4 : 0) + (transpose ? 4 : 0);
     const int64_t per_edge = 4 + (transpose ? 4 : 0);
     const int64_t tiles = (n + SG_TILE - 1) / SG_TILE + 1;
-    return sg_pool_agent_slots(n) * per_agent + nnz * per_edge + tiles * (int64_t)(sizeof(SgTile) + 4) +
+    const int64_t rowseg_bytes = (int64_t)SG_ROWSEG_CAPACITY(nnz) * (int64_t)sizeof(SgRowSeg); // the scatter's segment list
+    return sg_pool_agent_slots(n) * per_agent + nnz * per_edge + rowseg_bytes + tiles * (int64_t)(sizeof(SgTile) + 4) +
            (int64_t)sizeof(SgSeg);
 }
 
