@@ -219,9 +219,9 @@ __device__ __forceinline__ unsigned warp_dense_sirb(const int32_t (&k)[P], const
     return bits;
 }
 
-// Hybrid count step. Both step kernels are launched each tick; the one not
-// chosen returns at once. The choice reads the change totals of the two
-// previous ticks, which every block of both kernels sees alike. The loop form
+// Hybrid count step: whether tick r runs the busy-tick form (flat draws or the
+// loop form) instead of the class sweep. The choice reads the change totals of
+// the two previous ticks, which every block sees alike. The busy-tick form
 // pays a fixed cost per agent, the class sweep one per candidate; while an
 // epidemic grows, candidates (susceptible agents next to new infections, often
 // clustered around hubs) outnumber changes by far, so the loop form is chosen

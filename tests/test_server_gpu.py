@@ -66,9 +66,10 @@ def test_poll_and_take_result():
 
 def est_bytes(r):
     """About the server's footprint of a request (22 B per agent slot, 4 B per
-    CSR entry, tile and segment tables)."""
+    CSR entry, the scatter's segment list of 2 nnz / 64 + 64 entries of 16 B,
+    tile and segment tables)."""
     n, nnz = r["offsets"].size - 1, r["indices"].size
-    return ((n + 32) & ~31) * 22 + nnz * 4 + ((n + 2047) // 2048 + 1) * 20 + 256
+    return ((n + 32) & ~31) * 22 + nnz * 4 + (2 * nnz // 64 + 64) * 16 + ((n + 2047) // 2048 + 1) * 20 + 256
 
 
 def test_bad_csr_is_refused_on_both_submission_paths():
