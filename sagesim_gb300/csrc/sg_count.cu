@@ -1078,6 +1078,17 @@ static void count_step_flavour(const SgTickArgs &a, int flavour, int grid, cudaS
 #undef SG_CF
 }
 
+// Grid of the flat-draw (and merged hybrid) launches: two blocks per resident
+// slot of the current device, at most `grid`; 0 when the device is unknown.
+static int flat_grid(int grid)
+{
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        return 0;
+    return std::max(1, std::min(grid, 2 * kFlatBlocksPerSm * sms));
+}
+
 cudaError_t sg_launch_sir_count_step(const SgTickArgs &args, int variant, bool stats, bool inplace,
                                      int grid, cudaStream_t st, int *nlaunched)
 {
@@ -1089,11 +1100,8 @@ cudaError_t sg_launch_sir_count_step(const SgTickArgs &args, int variant, bool s
         // sweep and flat draws in one launch; the grid is the flat form's (two
         // blocks per resident slot), the sweep's groups are spread over it
         const int wpt = a.sweep_wpt == 2 || a.sweep_wpt == 4 ? a.sweep_wpt : 1;
-        int dev = 0, sms = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
-            return cudaErrorInvalidDevice;
-        const int hgrid = std::max(1, std::min(grid, 2 * kFlatBlocksPerSm * sms));
+        const int hgrid = flat_grid(grid);
+        if (hgrid <= 0) return cudaErrorInvalidDevice;
 #define SG_HY(V, S, W) launch_count_kernel(sir_count_hybrid_kernel<V, S, W>, a, hgrid, st)
 #define SG_HYW(V, S) (wpt == 1 ? SG_HY(V, S, 1) : wpt == 2 ? SG_HY(V, S, 2) : SG_HY(V, S, 4))
         if (variant == 1) {
@@ -1127,11 +1135,8 @@ cudaError_t sg_launch_sir_count_step(const SgTickArgs &args, int variant, bool s
         // flat draws take the busy ticks (or every tick without the hybrid); two
         // blocks per resident slot balance tiles of unequal cost better than
         // one wave of many-tile blocks or a block per tile
-        int dev = 0, sms = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
-            return cudaErrorInvalidDevice;
-        grid = std::max(1, std::min(grid, 2 * kFlatBlocksPerSm * sms));
+        grid = flat_grid(grid);
+        if (grid <= 0) return cudaErrorInvalidDevice;
         if (variant == 1) {
             if (stats) launch_count_kernel(sir_count_flat_kernel<1, true>, a, grid, st);
             else launch_count_kernel(sir_count_flat_kernel<1, false>, a, grid, st);
