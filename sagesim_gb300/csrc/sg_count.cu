@@ -1078,7 +1078,7 @@ static void count_step_flavour(const SgTickArgs &a, int flavour, int grid, cudaS
 #undef SG_CF
 }
 
-// Grid of the flat-draw (and merged hybrid) launches: two blocks per resident
+// Grid of the flat-draw (and merged hybrid) launches: three blocks per resident
 // slot of the current device, at most `grid`; 0 when the device is unknown.
 static int flat_grid(int grid)
 {
@@ -1086,7 +1086,7 @@ static int flat_grid(int grid)
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
         return 0;
-    return std::max(1, std::min(grid, 2 * kFlatBlocksPerSm * sms));
+    return std::max(1, std::min(grid, 3 * kFlatBlocksPerSm * sms));
 }
 
 cudaError_t sg_launch_sir_count_step(const SgTickArgs &args, int variant, bool stats, bool inplace,
@@ -1097,7 +1097,7 @@ cudaError_t sg_launch_sir_count_step(const SgTickArgs &args, int variant, bool s
     const bool sweep = (a.flavour & SG_FLAVOUR_SWEEP) && inplace && a.cls && a.chunks;
     if (!sweep) a.hybrid_rise = 0; // the loop form takes every tick
     if (sweep && a.hybrid_rise > 0 && (a.flavour & SG_FLAVOUR_FLAT)) {
-        // sweep and flat draws in one launch; the grid is the flat form's (two
+        // sweep and flat draws in one launch; the grid is the flat form's (three
         // blocks per resident slot), the sweep's groups are spread over it
         const int wpt = a.sweep_wpt == 2 || a.sweep_wpt == 4 ? a.sweep_wpt : 1;
         const int hgrid = flat_grid(grid);
@@ -1132,8 +1132,8 @@ cudaError_t sg_launch_sir_count_step(const SgTickArgs &args, int variant, bool s
         // hybrid: the busy-tick form too (it returns at once in sweep ticks)
     }
     if ((a.flavour & SG_FLAVOUR_FLAT) && inplace && a.chunks) {
-        // flat draws take the busy ticks (or every tick without the hybrid); two
-        // blocks per resident slot balance tiles of unequal cost better than
+        // flat draws take the busy ticks (or every tick without the hybrid); a
+        // few blocks per resident slot balance tiles of unequal cost better than
         // one wave of many-tile blocks or a block per tile
         grid = flat_grid(grid);
         if (grid <= 0) return cudaErrorInvalidDevice;
