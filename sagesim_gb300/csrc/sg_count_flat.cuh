@@ -15,9 +15,10 @@
 // draw j < k is below beta, so no order or early exit is needed). Hits are
 // bits in shared memory. Draws beyond kFlatCap of one candidate (hubs
 // surrounded by infected agents) are done afterwards, warp-wide, only for
-// those candidates still without a hit. The lane that owns an agent then
-// applies its transition exactly as the loop form does: state in place, class
-// byte, change-list entry and row. Warps balance their own draws and need no
+// those candidates still without a hit. The warp then lists its changed
+// agents in shared memory and each lane applies every 32nd transition exactly
+// as the loop form does: state in place, class byte, change-list entry and
+// row. Warps balance their own draws and need no
 // block barrier until the tile's change count is published; each warp's
 // changes go to its own 256-entry part of the tile's change list, announced to
 // the scatter as chunks of at most 32 (so this form needs the chunk list).
@@ -26,7 +27,7 @@
 // + 7, read as one 8-byte class load (or two 16-byte state loads without class
 // bytes), two 16-byte count loads and two 16-byte key loads issued together.
 constexpr int32_t kFlatCap = 32;
-constexpr int kFlatBlocksPerSm = 5;            // resident blocks: 48 registers, 29 KB shared memory each
+constexpr int kFlatBlocksPerSm = 5;            // resident blocks: 48 registers, 33 KB shared memory each
 constexpr int kFlatPer = SG_TILE / SG_SIR_THREADS;
 constexpr int kFlatIlp = 4;                    // draws a lane evaluates side by side
 constexpr int kFlatWarpAgents = 32 * kFlatPer; // agents (and at most candidates) per warp
