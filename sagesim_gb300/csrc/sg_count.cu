@@ -542,7 +542,7 @@ __device__ __forceinline__ void sweep_tick(const SgTickArgs &a, SgSweepSmem<WPT>
     constexpr int kRuns = SG_TILE / (32 * kRun); // runs of a whole tile per lane
     constexpr int kMyRuns = kRuns / WPT;         // runs of this warp's part of a tile
     constexpr int TPB = kWarps / WPT;            // tiles per block (group)
-    constexpr int U = 4;                         // candidates per thread in flight
+    constexpr int U = 2;                         // candidates per thread in flight (2: less divergence than 4)
     static_assert(kRuns * 32 * kRun == SG_TILE, "runs must cover the tile");
     static_assert(kMyRuns * WPT == kRuns && TPB * WPT == kWarps, "warps must split tiles evenly");
     static_assert(SG_TILE <= 0x800, "slot must fit in 11 bits");
