@@ -48,7 +48,7 @@ SEED = 1
 #       --csv --log-file dram.csv python bench.py --profile-case
 # keyed by (strategy, agents, kernel); the count step is one launch per tick (class
 # sweep or flat draws). Re-measure when a kernel changes.
-MEASURED_TRAFFIC = {("count", 10_000_000, "sir_count_step"): 28.197e6}
+MEASURED_TRAFFIC = {("count", 10_000_000, "sir_count_step"): 27.999e6}
 PARTS = 64
 CODES = (1, 2, 3)
 WORKLOAD = ("SIR per-infected-neighbour (salt 2+j trials), BA n=%d m=4 seed 1, 64-way locality relabel, "
